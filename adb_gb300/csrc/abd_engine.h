@@ -1,0 +1,145 @@
+// Internal declarations shared by the CUDA translation units of libabd_gb300.so:
+// device buffers, the pair-set layout in HBM, and the host-side launchers of each stage.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/abd_gb300.h"
+
+namespace abd {
+
+struct CudaError {
+  cudaError_t code;
+  std::string where;
+};
+void check(cudaError_t e, const char* where);  // throws CudaError
+#define CK(x) ::abd::check((x), #x)
+
+// Grow-only device buffer (contents are not preserved on growth unless asked).
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t n, bool keep = false, size_t keep_n = 0) {
+    if (n <= cap) return;
+    size_t nc = cap ? cap : 1024;
+    while (nc < n) nc = nc + nc / 2 + 1;
+    T* np_ = nullptr;
+    CK(cudaMalloc(&np_, nc * sizeof(T)));
+    if (keep && p && keep_n) CK(cudaMemcpy(np_, p, keep_n * sizeof(T), cudaMemcpyDeviceToDevice));
+    if (p) CK(cudaFree(p));
+    p = np_;
+    cap = nc;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Read-only geometry and state pointers passed by value to the kernels.
+struct Geo {
+  int nb, nv, ne, nf;
+  const int *v_off, *e_off, *f_off;     // nb + 1
+  const double* rest;                   // nv * 3 (x, y, z per vertex)
+  const int* vbody;                     // nv
+  const int* ev;                        // ne * 2 global vertex ids
+  const int* fv;                        // nf * 3 global vertex ids
+  const double* mass;                   // nb
+  const double* Ic;                     // nb
+  const double* rest_box;               // nb * 6 (lo, hi), inflated by sqrt(dhat)
+  const int *scene_beg, *scene_end;     // nb: body range of this body's scene
+  const double *q, *dq, *q0, *dqdt;     // nb * 12
+  double *X, *Xq, *X0;                  // 3 * nv, structure of arrays (x | y | z)
+};
+
+// A culled pair set together with the overlap structure it was built on.
+struct PairSet {
+  int nov = 0, nnz = 0, npt = 0, nee = 0, nvg = 0;
+  // symmetric overlap CSR over bodies (both (I,J) and (J,I)); upidx -> unique overlap
+  DBuf<int> row_ptr, col, upidx;
+  DBuf<int> ovI, ovJ;                   // unique overlaps, I < J, sorted
+  DBuf<int> pt, ee;                     // 4 ints per pair: body A, prim A, body B, prim B
+  DBuf<int8_t> pt_ty, ee_ty;
+  DBuf<int> pt_ov, ee_ov;               // overlap of each pair
+  DBuf<int> vg;                         // 2 ints per pair: body, local vertex
+  DBuf<int> vg_seg;                     // nb + 1: VG pairs of each body
+  // lagged friction of the pairs (valid after an assembly on this set)
+  DBuf<double> pt_lag, ee_lag;          // 11 per pair, SoA: c0(3) c1(3) gamma(4) lambda
+  DBuf<double> vg_lam;
+};
+
+struct Params {
+  double dhat, kappa, d_sqrt, eps_x, ortho_kappa, ground_offset, dt, gravity_y;
+  double mu, epsv, max_uk;
+  int psd, pt_fric, ee_fric, vg_fric, ground, pt, ee;
+};
+
+// Culling scratch shared by all culls of a handle.
+struct CullScratch {
+  DBuf<double> bbox;
+  DBuf<int> cnt_all, cnt_up, up_ptr, rowid;
+  DBuf<double> ovcull;
+  DBuf<float> ovcull_f;
+  DBuf<float> vbox, ebox, fbox;
+  DBuf<int> bin_cnt, bin_off, lst;
+  DBuf<long long> cand_cnt, cand_off;
+  DBuf<uint8_t> flags;
+  DBuf<int> blk_a, blk_b, blk_a_off, blk_b_off;
+  DBuf<int> vflag_cnt, vflag_off;
+  DBuf<unsigned long long> toi_key;     // [0] pt/ee, [1] ground
+  DBuf<int> tmp_int;
+  DBuf<long long> tmp_ll;
+  int* h_small = nullptr;               // pinned host scratch
+  long long* h_ll = nullptr;
+  unsigned long long* h_toi = nullptr;
+};
+
+// ---------------- scan ----------------
+void scan_exclusive_int(const int* in, int* out, int n, int* d_total, cudaStream_t s, DBuf<int>& tmp);
+void scan_exclusive_ll(const long long* in, long long* out, int n, long long* d_total, cudaStream_t s,
+                       DBuf<long long>& tmp);
+
+// ---------------- culling (cull.cu) ----------------
+void launch_project(const Geo& g, int which, double alpha, cudaStream_t s);
+// vtn 1/2: builds `out`; vtn 3: returns the TOIs (pt/ee, ground) through *toi_p, *toi_g.
+void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs, PairSet& out, double* toi_p,
+          double* toi_g, cudaStream_t s);
+
+// ---------------- Newton system (newton.cu) ----------------
+enum { CONTRIB = 456 };  // dI(144) dJ(144) off(144) gI(12) gJ(12)
+struct NewtonBufs {
+  DBuf<double> pt_c, ee_c;   // CONTRIB per pair (SoA)
+  DBuf<int> pt_seg, ee_seg;  // nov + 1
+  DBuf<double> ovr;          // nov * CONTRIB
+  DBuf<int> has;             // nov
+  DBuf<double> D, Dinv, grad;
+  DBuf<double> x, r, z, p, qv, partial;
+  DBuf<double> red;          // small reductions
+  DBuf<int> status;          // [0] solver status, [1] pcg iters
+  double* h_red = nullptr;   // pinned
+  int* h_int = nullptr;
+};
+void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& nb, cudaStream_t s);
+// Solves H x = grad; returns iterations (negative on breakdown). dq = -x written to g.dq.
+int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& nb, double rel_tol, int max_iter, double* dq, cudaStream_t s,
+              int* status);
+// Line-search energy at the trial configuration (X must hold q + alpha dq):
+// inertia + barrier over `Snew` + lagged friction over `Slag`.
+double energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_barrier_inertia,
+              NewtonBufs& nb, cudaStream_t s);
+// dots over the 12 nb dofs: out[0] = dq.grad, out[1] = |grad|^2, out[2] = |dq|^2
+void dots(int n, const double* dq, const double* grad, NewtonBufs& nb, double* out, cudaStream_t s);
+void launch_scale(double* v, int n, double s, cudaStream_t st);
+void launch_q_update(double* q, const double* dq, int n, double alpha, cudaStream_t st);
+void launch_frame_end(double* q, double* q0, double* dqdt, int n, double dt, cudaStream_t st);
+void launch_copy(double* dst, const double* src, int n, cudaStream_t st);
+
+// ---------------- per-primitive batches (prims.cu) ----------------
+double measure_fp64_gflops();
+
+}  // namespace abd

@@ -1,0 +1,480 @@
+// Per-pair IPC terms on the device: barrier energy, gradient and PSD-projected Hessian
+// of one point-triangle or edge-edge pair, lagged friction, and the chain rule onto the
+// 12 affine DOFs of the two bodies.
+//
+// The reference forms the 12x12 vertex-space Hessian H = b'' g g^T + b' hess(d) (plus
+// the edge-edge mollifier terms), projects it to PSD with a full eigen-decomposition
+// (model/psd.h:5-33, called from model/core_ipc.cpp:40,79), adds friction
+// (model/friction.cpp:15-47) and multiplies by the Jacobians of x = A xbar + p
+// (model/pt_ipc.cpp:153-169, model/ee_ipc.cpp:180-196).
+//
+// Here the same quantities are built without ever forming H in vertex space. Every
+// squared distance d(x) is invariant under a common translation of the four points,
+// so H lives in the 9-dimensional translation-free subspace spanned by Q (x) I3 with
+//   Q = [(1,-1,0,0)/sqrt2, (0,0,1,-1)/sqrt2, (1,1,-1,-1)/2]  (orthonormal, _|_ (1,1,1,1)).
+// H is assembled directly as the 9x9 matrix S = (Q (x) I)^T H (Q (x) I) from its
+// rank-structured pieces, S is eigen-projected (cyclic Jacobi), friction is added in
+// the same coordinates (the friction stencil also sums to zero), and the body blocks are
+// Y_A S Y_B^T with Y_b[k][a] = sum_{i on body b} xbar~_i[k] Q[i][a]. Because Q is
+// orthonormal, projecting S is exactly projecting H (same eigenvalues, eigenvectors
+// mapped by Q (x) I), so the result equals the reference's up to rounding.
+#pragma once
+#include "abd_exact.cuh"
+
+namespace abd {
+
+#define DEV __device__ __forceinline__
+
+struct BarrierP {
+  double dhat, kappa;
+};
+
+DEV double barrier_b(double d, const BarrierP& p) {
+  if (d >= p.dhat) return 0.0;
+  return p.kappa * -(d - p.dhat) * (d - p.dhat) * log(d / p.dhat) / (p.dhat * p.dhat);
+}
+DEV double barrier_b2(double d, const BarrierP& p) {
+  if (d >= p.dhat) return 0.0;
+  double dh = p.dhat;
+  return -p.kappa * (2 * log(d / dh) + (d - dh) / d + (d - dh) * (2 / d + dh / d / d)) / (dh * dh);
+}
+DEV double barrier_b1(double x, const BarrierP& p) {
+  if (x >= p.dhat) return 0.0;
+  double dh = p.dhat;
+  return -(x - dh) * p.kappa * (2 * log(x / dh) + (x - dh) / x) / (dh * dh);
+}
+
+DEV double f0_SF(double x, double epsv) {
+  if (fabs(x) >= epsv) return x;
+  return x * x * (-x / (3 * epsv) + 1) / epsv + epsv / 3;
+}
+DEV double f1_SF_over_x(double x, double epsv) {
+  if (fabs(x) >= epsv) return 1 / x;
+  return (-x + 2 * epsv) / (epsv * epsv);
+}
+
+// Squared-distance stencil: d = |w|^2, w = sum_i c_i x_i at the optimal closest-point
+// parameters; a_k = dc/dbeta_k for the m free parameters.
+struct Stencil {
+  double c[4];
+  double a[2][4];
+  int m;
+};
+
+DEV d3 fd3(double x, double y, double z) { return d3{x, y, z}; }
+DEV d3 fadd(d3 a, d3 b) { return fd3(a.x + b.x, a.y + b.y, a.z + b.z); }
+DEV d3 fsub(d3 a, d3 b) { return fd3(a.x - b.x, a.y - b.y, a.z - b.z); }
+DEV d3 fscl(double s, d3 a) { return fd3(s * a.x, s * a.y, s * a.z); }
+DEV double fdot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+DEV d3 fcross(d3 a, d3 b) { return fd3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+DEV d3 fnormalized(d3 a) { return fscl(1.0 / sqrt(fdot(a, a)), a); }
+DEV double c3(d3 a, int r) { return r == 0 ? a.x : (r == 1 ? a.y : a.z); }
+
+DEV void st_clear(Stencil& s) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    s.c[i] = 0;
+    s.a[0][i] = 0;
+    s.a[1][i] = 0;
+  }
+  s.m = 0;
+}
+DEV void st_pp(int P, int Q_, Stencil& s) {
+  st_clear(s);
+  s.c[P] = 1;
+  s.c[Q_] = -1;
+}
+DEV void st_pe(const d3* X, int P, int E0, int E1, Stencil& s) {
+  st_clear(s);
+  d3 e = fsub(X[E1], X[E0]);
+  double t = fdot(fsub(X[P], X[E0]), e) / fdot(e, e);
+  s.c[P] = 1;
+  s.c[E0] = -(1 - t);
+  s.c[E1] = -t;
+  s.m = 1;
+  s.a[0][E0] = 1;
+  s.a[0][E1] = -1;
+}
+DEV void st_pt(const d3* X, int ty, Stencil& s) {
+  switch (ty) {
+    case P_T0: st_pp(0, 1, s); return;
+    case P_T1: st_pp(0, 2, s); return;
+    case P_T2: st_pp(0, 3, s); return;
+    case P_E0: st_pe(X, 0, 1, 2, s); return;
+    case P_E1: st_pe(X, 0, 2, 3, s); return;
+    case P_E2: st_pe(X, 0, 3, 1, s); return;
+    default: {
+      st_clear(s);
+      d3 e1 = fsub(X[2], X[1]), e2 = fsub(X[3], X[1]), r = fsub(X[0], X[1]);
+      double g11 = fdot(e1, e1), g12 = fdot(e1, e2), g22 = fdot(e2, e2);
+      double det = g11 * g22 - g12 * g12;
+      double r1 = fdot(e1, r), r2 = fdot(e2, r);
+      double b1 = (g22 * r1 - g12 * r2) / det, b2 = (g11 * r2 - g12 * r1) / det;
+      s.c[0] = 1;
+      s.c[1] = -(1 - b1 - b2);
+      s.c[2] = -b1;
+      s.c[3] = -b2;
+      s.m = 2;
+      s.a[0][1] = 1; s.a[0][2] = -1;
+      s.a[1][1] = 1; s.a[1][3] = -1;
+    }
+  }
+}
+DEV void st_ee(const d3* X, int ty, Stencil& s) {
+  switch (ty) {
+    case EA0_EB0: st_pp(0, 2, s); return;
+    case EA0_EB1: st_pp(0, 3, s); return;
+    case EA1_EB0: st_pp(1, 2, s); return;
+    case EA1_EB1: st_pp(1, 3, s); return;
+    case EA_EB0: st_pe(X, 2, 0, 1, s); return;
+    case EA_EB1: st_pe(X, 3, 0, 1, s); return;
+    case EA0_EB: st_pe(X, 0, 2, 3, s); return;
+    case EA1_EB: st_pe(X, 1, 2, 3, s); return;
+    default: {
+      st_clear(s);
+      d3 u = fsub(X[1], X[0]), v = fsub(X[3], X[2]), w0 = fsub(X[0], X[2]);
+      double a = fdot(u, u), b = fdot(u, v), c = fdot(v, v), d = fdot(u, w0), e = fdot(v, w0);
+      double D = a * c - b * b;
+      double sp = (b * e - c * d) / D, tp = (a * e - b * d) / D;
+      s.c[0] = 1 - sp;
+      s.c[1] = sp;
+      s.c[2] = -(1 - tp);
+      s.c[3] = -tp;
+      s.m = 2;
+      s.a[0][0] = -1; s.a[0][1] = 1;
+      s.a[1][2] = 1; s.a[1][3] = -1;
+    }
+  }
+}
+
+// Q^T u for a 4-vector u.
+DEV void qt4(const double* u, double* o) {
+  const double r2 = 0.70710678118654752440;
+  o[0] = (u[0] - u[1]) * r2;
+  o[1] = (u[2] - u[3]) * r2;
+  o[2] = 0.5 * ((u[0] + u[1]) - (u[2] + u[3]));
+}
+DEV double Qe(int i, int a) {
+  const double r2 = 0.70710678118654752440;
+  if (a == 0) return i == 0 ? r2 : (i == 1 ? -r2 : 0.0);
+  if (a == 1) return i == 2 ? r2 : (i == 3 ? -r2 : 0.0);
+  return i < 2 ? 0.5 : -0.5;
+}
+
+// Symmetric eigen-projection of an n x n matrix in place (cyclic Jacobi, n <= 9).
+template <int N>
+DEV void psd_project(double (&S)[N][N]) {
+  double A[N][N], V[N][N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      A[i][j] = 0.5 * (S[i][j] + S[j][i]);
+      V[i][j] = (i == j) ? 1.0 : 0.0;
+    }
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    double off = 0, tot = 0;
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        double v = A[i][j] * A[i][j];
+        tot += v;
+        if (i != j) off += v;
+      }
+    if (off <= 1e-32 * tot || off == 0.0) break;
+    for (int p = 0; p < N - 1; ++p)
+      for (int q = p + 1; q < N; ++q) {
+        double apq = A[p][q];
+        if (apq == 0.0) continue;
+        double theta = (A[q][q] - A[p][p]) / (2 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
+        double c = 1 / sqrt(t * t + 1), s = t * c;
+        for (int k = 0; k < N; ++k) {
+          double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - s * akq;
+          A[k][q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < N; ++k) {
+          double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - s * aqk;
+          A[q][k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < N; ++k) {
+          double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - s * vkq;
+          V[k][q] = s * vkp + c * vkq;
+        }
+        A[p][q] = 0.0;
+        A[q][p] = 0.0;
+      }
+  }
+  bool neg = false;
+  double lam[N];
+  for (int i = 0; i < N; ++i) {
+    lam[i] = A[i][i];
+    if (lam[i] < 0.0) neg = true;
+  }
+  if (!neg) return;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      double s = 0;
+      for (int k = 0; k < N; ++k)
+        if (lam[k] > 0) s += V[i][k] * lam[k] * V[j][k];
+      S[i][j] = s;
+    }
+}
+
+// Friction stencil of a pair: tangent basis (c0, c1), relative-displacement weights
+// gamma (model/pt_ipc.cpp:22-107, model/ee_ipc.cpp:21-118).
+struct FrictionFrame {
+  d3 c0, c1;
+  double gam[4];
+};
+
+DEV void pp_basis(d3 p0, d3 p1, FrictionFrame& f) {
+  d3 d = fsub(p1, p0);
+  d3 cx = fcross(fd3(1, 0, 0), d), cy = fcross(fd3(0, 1, 0), d);
+  if (fdot(cx, cx) > fdot(cy, cy)) {
+    f.c0 = fnormalized(cx);
+    f.c1 = fnormalized(fcross(d, cx));
+  } else {
+    f.c0 = fnormalized(cy);
+    f.c1 = fnormalized(fcross(d, cy));
+  }
+}
+DEV void pe_basis(d3 p, d3 e0, d3 e1, FrictionFrame& f) {
+  d3 e = fsub(e1, e0);
+  f.c0 = fnormalized(e);
+  f.c1 = fnormalized(fcross(e, fsub(p, e0)));
+}
+DEV double pe_closest(d3 p, d3 e0, d3 e1) {
+  d3 e = fsub(e1, e0);
+  return fdot(fsub(p, e0), e) / fdot(e, e);
+}
+DEV void frame_pt(const d3* X, int ty, FrictionFrame& f) {
+  double l0, l1;
+  {
+    d3 b0 = fsub(X[2], X[1]), b1 = fsub(X[3], X[1]), r = fsub(X[0], X[1]);
+    solve2_ldlt(fdot(b0, b0), fdot(b0, b1), fdot(b1, b1), fdot(b0, r), fdot(b1, r), l0, l1);
+  }
+  double tl[3] = {1 - l0 - l1, l0, l1};
+  {
+    d3 e0 = fsub(X[2], X[1]);
+    d3 n = fcross(e0, fsub(X[3], X[1]));
+    f.c0 = fnormalized(e0);
+    f.c1 = fnormalized(fcross(n, e0));
+  }
+  switch (ty) {
+    case P_T0: pp_basis(X[0], X[1], f); tl[0] = 1; tl[1] = 0; tl[2] = 0; break;
+    case P_T1: pp_basis(X[0], X[2], f); tl[0] = 0; tl[1] = 1; tl[2] = 0; break;
+    case P_T2: pp_basis(X[0], X[3], f); tl[0] = 0; tl[1] = 0; tl[2] = 1; break;
+    case P_E0: { double e = pe_closest(X[0], X[1], X[2]); tl[0] = 1 - e; tl[1] = e; tl[2] = 0; pe_basis(X[0], X[1], X[2], f); break; }
+    case P_E1: { double e = pe_closest(X[0], X[2], X[3]); tl[0] = 0; tl[1] = 1 - e; tl[2] = e; pe_basis(X[0], X[2], X[3], f); break; }
+    case P_E2: { double e = pe_closest(X[0], X[3], X[1]); tl[0] = e; tl[1] = 0; tl[2] = 1 - e; pe_basis(X[0], X[3], X[1], f); break; }
+    default: break;
+  }
+  f.gam[0] = -1.0;
+  f.gam[1] = tl[0];
+  f.gam[2] = tl[1];
+  f.gam[3] = tl[2];
+}
+DEV void frame_ee(const d3* X, int ty, FrictionFrame& f) {
+  double s, t;
+  {
+    d3 w = fsub(X[0], X[2]), ea = fsub(X[1], X[0]), eb = fsub(X[3], X[2]);
+    solve2_ldlt(fdot(ea, ea), -fdot(eb, ea), fdot(eb, eb), -fdot(w, ea), fdot(w, eb), s, t);
+  }
+  {
+    d3 ea = fsub(X[1], X[0]);
+    d3 n = fcross(ea, fsub(X[3], X[2]));
+    f.c0 = fnormalized(ea);
+    f.c1 = fnormalized(fcross(n, ea));
+  }
+  switch (ty) {
+    case EA0_EB0: pp_basis(X[0], X[2], f); s = 0; t = 0; break;
+    case EA0_EB1: pp_basis(X[0], X[3], f); s = 0; t = 1; break;
+    case EA1_EB0: pp_basis(X[1], X[2], f); s = 1; t = 0; break;
+    case EA1_EB1: pp_basis(X[1], X[3], f); s = 1; t = 1; break;
+    case EA_EB0: s = pe_closest(X[2], X[0], X[1]); t = 0; pe_basis(X[2], X[0], X[1], f); break;
+    case EA_EB1: s = pe_closest(X[3], X[0], X[1]); t = 1; pe_basis(X[3], X[0], X[1], f); break;
+    case EA0_EB: s = 0; t = pe_closest(X[0], X[2], X[3]); pe_basis(X[0], X[2], X[3], f); break;
+    case EA1_EB: s = 1; t = pe_closest(X[1], X[2], X[3]); pe_basis(X[1], X[2], X[3], f); break;
+    default: break;
+  }
+  s = fmax(fmin(1.0, s), 0.0);
+  t = fmax(fmin(1.0, t), 0.0);
+  f.gam[0] = -(1 - s);
+  f.gam[1] = -s;
+  f.gam[2] = 1 - t;
+  f.gam[3] = t;
+}
+
+struct FrictionP {
+  double mu, epsv, max_uk;
+};
+
+// 2x2 friction Hessian factor M and gradient scale (friction.cpp:15-47):
+// g += gamma (x) (mu lam f1 P uk), H += (gamma gamma^T) (x) (P M P^T).
+DEV void friction_2x2(const double* uk2, double lam, const FrictionP& fp, double& gscale, double M[2][2]) {
+  double uk = sqrt(uk2[0] * uk2[0] + uk2[1] * uk2[1]);
+  double f1 = f1_SF_over_x(uk, fp.epsv);
+  gscale = fp.mu * lam * f1;
+  if (uk >= fp.epsv) {
+    double ut[2] = {-uk2[1], uk2[0]};
+    double sc = fp.mu * lam * f1 / (uk * uk);
+    for (int a = 0; a < 2; ++a)
+      for (int b = 0; b < 2; ++b) M[a][b] = sc * ut[a] * ut[b];
+  } else if (uk <= fp.max_uk) {
+    double sc = fp.mu * lam * f1;
+    M[0][0] = sc; M[1][1] = sc; M[0][1] = M[1][0] = 0;
+  } else {
+    double f2 = -1.0 / (fp.epsv * fp.epsv);
+    double m00 = f2 / uk * uk2[0] * uk2[0] + f1, m11 = f2 / uk * uk2[1] * uk2[1] + f1, m01 = f2 / uk * uk2[0] * uk2[1];
+    double s = fp.mu * lam;
+    m00 *= s; m11 *= s; m01 *= s;
+    // closed-form 2x2 eigen-projection
+    double tr = 0.5 * (m00 + m11), df = 0.5 * (m00 - m11);
+    double rad = sqrt(df * df + m01 * m01);
+    double l0 = tr - rad, l1 = tr + rad;
+    if (l0 >= 0.0) {
+      M[0][0] = m00; M[1][1] = m11; M[0][1] = M[1][0] = m01;
+    } else {
+      // eigenvector of l1
+      double vx, vy;
+      if (rad == 0.0) { vx = 1; vy = 0; }
+      else if (df >= 0) { vx = df + rad; vy = m01; }
+      else { vx = m01; vy = rad - df; }
+      double n = sqrt(vx * vx + vy * vy);
+      vx /= n; vy /= n;
+      double l = l1 > 0 ? l1 : 0.0;
+      M[0][0] = l * vx * vx; M[1][1] = l * vy * vy; M[0][1] = M[1][0] = l * vx * vy;
+    }
+  }
+}
+
+// Reduced 9x9 Hessian S of a pair. Returns the vertex-space gradient g[4] (3-vectors).
+// kind 0: point-triangle, 1: edge-edge (mollified when the edges are near parallel).
+DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& bp, double eps_x_param, bool psd,
+                      double (&S)[9][9], d3* g) {
+  Stencil st;
+  if (kind == 0) st_pt(X, ty, st);
+  else st_ee(X, ty, st);
+  d3 w = fd3(0, 0, 0), W[2] = {fd3(0, 0, 0), fd3(0, 0, 0)};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    w = fadd(w, fscl(st.c[i], X[i]));
+    W[0] = fadd(W[0], fscl(st.a[0][i], X[i]));
+    W[1] = fadd(W[1], fscl(st.a[1][i], X[i]));
+  }
+  double Gi[2][2] = {{0, 0}, {0, 0}};
+  if (st.m == 1) {
+    Gi[0][0] = 1.0 / (2 * fdot(W[0], W[0]));
+  } else if (st.m == 2) {
+    double g00 = 2 * fdot(W[0], W[0]), g01 = 2 * fdot(W[0], W[1]), g11 = 2 * fdot(W[1], W[1]);
+    double det = g00 * g11 - g01 * g01;
+    Gi[0][0] = g11 / det;
+    Gi[1][1] = g00 / det;
+    Gi[0][1] = Gi[1][0] = -g01 / det;
+  }
+  double ch[3], ah[2][3];
+  qt4(st.c, ch);
+  qt4(st.a[0], ah[0]);
+  qt4(st.a[1], ah[1]);
+  double Phi[2][9];
+  double gd[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      gd[3 * a + r] = 2 * ch[a] * c3(w, r);
+      Phi[0][3 * a + r] = 2 * (ch[a] * c3(W[0], r) + ah[0][a] * c3(w, r));
+      Phi[1][3 * a + r] = 2 * (ch[a] * c3(W[1], r) + ah[1][a] * c3(w, r));
+    }
+  double B1 = barrier_b1(d, bp), B2 = barrier_b2(d, bp);
+  double mol = 1.0, B = 0.0, m1 = 0.0, m2 = 0.0;
+  double gx[9];
+  double Hx[9][9];
+  bool mollified = false;
+  d3 gu = fd3(0, 0, 0), gv = fd3(0, 0, 0);
+  if (kind == 1) {
+    d3 u = fsub(X[1], X[0]), v = fsub(X[3], X[2]);
+    double eps_x = eps_x_param * fdot(fsub(X[0], X[1]), fsub(X[0], X[1])) * fdot(fsub(X[2], X[3]), fsub(X[2], X[3]));
+    d3 cr = fcross(u, v);
+    double x = fdot(cr, cr);
+    if (x < eps_x) {
+      mollified = true;
+      double xe = x / eps_x;
+      mol = (-xe + 2.0) * xe;
+      m1 = 2.0 * (1.0 - xe) / eps_x;
+      m2 = -2.0 / (eps_x * eps_x);
+      B = barrier_b(d, bp);
+      double uu = fdot(u, u), vv = fdot(v, v), uv = fdot(u, v);
+      gu = fsub(fscl(2.0 * vv, u), fscl(2.0 * uv, v));
+      gv = fsub(fscl(2.0 * uu, v), fscl(2.0 * uv, u));
+      const double sq2 = 1.41421356237309504880;
+      for (int r = 0; r < 3; ++r) {
+        gx[r] = -sq2 * c3(gu, r);
+        gx[3 + r] = -sq2 * c3(gv, r);
+        gx[6 + r] = 0.0;
+      }
+      for (int i = 0; i < 9; ++i)
+        for (int j = 0; j < 9; ++j) Hx[i][j] = 0.0;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double dij = (i == j) ? 1.0 : 0.0;
+          double huu = 2.0 * (vv * dij - c3(v, i) * c3(v, j));
+          double hvv = 2.0 * (uu * dij - c3(u, i) * c3(u, j));
+          double huv = 2.0 * (2.0 * c3(u, i) * c3(v, j) - c3(v, i) * c3(u, j) - uv * dij);
+          double hvu = 2.0 * (2.0 * c3(u, j) * c3(v, i) - c3(v, j) * c3(u, i) - uv * dij);
+          Hx[i][j] = 2.0 * huu;
+          Hx[3 + i][3 + j] = 2.0 * hvv;
+          Hx[i][3 + j] = 2.0 * huv;
+          Hx[3 + i][j] = 2.0 * hvu;
+        }
+    }
+  }
+  for (int p = 0; p < 9; ++p)
+    for (int q = 0; q < 9; ++q) {
+      int a = p / 3, r = p % 3, b = q / 3, s = q % 3;
+      double hd = (r == s ? 2 * ch[a] * ch[b] : 0.0);
+      for (int k = 0; k < st.m; ++k)
+        for (int l = 0; l < st.m; ++l) hd -= Phi[k][p] * Gi[k][l] * Phi[l][q];
+      double h = mol * (B2 * gd[p] * gd[q] + B1 * hd);
+      if (mollified) {
+        double gmp = m1 * gx[p], gmq = m1 * gx[q];
+        h += (m2 * gx[p] * gx[q] + m1 * Hx[p][q]) * B + B1 * (gmp * gd[q] + gd[p] * gmq);
+      }
+      S[p][q] = h;
+    }
+  if (psd) psd_project<9>(S);
+  // vertex-space gradient: mol b' grad d + b grad mol
+#pragma unroll
+  for (int i = 0; i < 4; ++i) g[i] = fscl(mol * B1 * 2 * st.c[i], w);
+  if (mollified) {
+    g[0] = fsub(g[0], fscl(B * m1, gu));
+    g[1] = fadd(g[1], fscl(B * m1, gu));
+    g[2] = fsub(g[2], fscl(B * m1, gv));
+    g[3] = fadd(g[3], fscl(B * m1, gv));
+  }
+}
+
+// Adds friction to the reduced Hessian and to the vertex gradient.
+DEV void pair_friction(const FrictionFrame& fr, const double* uk, double lam, const FrictionP& fp, double (&S)[9][9],
+                       d3* g) {
+  double gs, M[2][2];
+  friction_2x2(uk, lam, fp, gs, M);
+  d3 F = fadd(fscl(gs * uk[0], fr.c0), fscl(gs * uk[1], fr.c1));
+#pragma unroll
+  for (int i = 0; i < 4; ++i) g[i] = fadd(g[i], fscl(fr.gam[i], F));
+  double N[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int s = 0; s < 3; ++s) {
+      double p0r = c3(fr.c0, r), p1r = c3(fr.c1, r), p0s = c3(fr.c0, s), p1s = c3(fr.c1, s);
+      N[r][s] = p0r * (M[0][0] * p0s + M[0][1] * p1s) + p1r * (M[1][0] * p0s + M[1][1] * p1s);
+    }
+  double gh[3];
+  qt4(fr.gam, gh);
+  for (int p = 0; p < 9; ++p)
+    for (int q = 0; q < 9; ++q) S[p][q] += gh[p / 3] * gh[q / 3] * N[p % 3][q % 3];
+}
+
+}  // namespace abd

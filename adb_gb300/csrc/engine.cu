@@ -1,0 +1,513 @@
+// Host side of the GB300 step: the handle, its device buffers, the per-frame Newton
+// loop (the reference's ABD::implicit_euler, model/abd.cpp:30-140, with ccd() :142-196
+// and line_search(dt) :198-227 / model/line_search.cpp:39-136) and the C ABI.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "abd_engine.h"
+
+namespace abd {
+
+void check(cudaError_t e, const char* where) {
+  if (e != cudaSuccess) throw CudaError{e, where};
+}
+
+struct Engine {
+  abd_config cfg;
+  Params P;
+  int nb = 0, nv = 0, ne = 0, nf = 0;
+  cudaStream_t s = nullptr;
+  DBuf<int> v_off, e_off, f_off, vbody, ev, fv, scene_beg, scene_end;
+  DBuf<double> rest, mass, Ic, rest_box, q, q0, dqdt, dq, X, Xq, X0;
+  PairSet sets[3];
+  int cur = 0;
+  CullScratch cs;
+  NewtonBufs nbufs;
+  int iter = 0, g_cnt = 0, p_cnt = 0;
+  int last_cull_set = 0;
+  std::string err;
+
+  Geo geo() const {
+    Geo g;
+    g.nb = nb; g.nv = nv; g.ne = ne; g.nf = nf;
+    g.v_off = v_off.p; g.e_off = e_off.p; g.f_off = f_off.p;
+    g.rest = rest.p; g.vbody = vbody.p; g.ev = ev.p; g.fv = fv.p;
+    g.mass = mass.p; g.Ic = Ic.p; g.rest_box = rest_box.p;
+    g.scene_beg = scene_beg.p; g.scene_end = scene_end.p;
+    g.q = q.p; g.dq = dq.p; g.q0 = q0.p; g.dqdt = dqdt.p;
+    g.X = X.p; g.Xq = Xq.p; g.X0 = X0.p;
+    return g;
+  }
+
+  ~Engine() {
+    DBuf<int>* ib[] = {&v_off, &e_off, &f_off, &vbody, &ev, &fv, &scene_beg, &scene_end};
+    for (auto* b : ib) b->release();
+    DBuf<double>* db[] = {&rest, &mass, &Ic, &rest_box, &q, &q0, &dqdt, &dq, &X, &Xq, &X0};
+    for (auto* b : db) b->release();
+    for (auto& S : sets) {
+      S.row_ptr.release(); S.col.release(); S.upidx.release(); S.ovI.release(); S.ovJ.release();
+      S.pt.release(); S.ee.release(); S.pt_ty.release(); S.ee_ty.release(); S.pt_ov.release(); S.ee_ov.release();
+      S.vg.release(); S.vg_seg.release(); S.pt_lag.release(); S.ee_lag.release(); S.vg_lam.release();
+    }
+    cs.bbox.release(); cs.cnt_all.release(); cs.cnt_up.release(); cs.up_ptr.release(); cs.rowid.release();
+    cs.ovcull.release(); cs.ovcull_f.release(); cs.vbox.release(); cs.ebox.release(); cs.fbox.release();
+    cs.bin_cnt.release(); cs.bin_off.release(); cs.lst.release(); cs.cand_cnt.release(); cs.cand_off.release();
+    cs.flags.release(); cs.blk_a.release(); cs.blk_b.release(); cs.blk_a_off.release(); cs.blk_b_off.release();
+    cs.vflag_cnt.release(); cs.vflag_off.release(); cs.toi_key.release(); cs.tmp_int.release(); cs.tmp_ll.release();
+    if (cs.h_small) cudaFreeHost(cs.h_small);
+    if (cs.h_ll) cudaFreeHost(cs.h_ll);
+    if (cs.h_toi) cudaFreeHost(cs.h_toi);
+    nbufs.pt_c.release(); nbufs.ee_c.release(); nbufs.pt_seg.release(); nbufs.ee_seg.release();
+    nbufs.ovr.release(); nbufs.has.release(); nbufs.D.release(); nbufs.Dinv.release(); nbufs.grad.release();
+    nbufs.x.release(); nbufs.r.release(); nbufs.z.release(); nbufs.p.release(); nbufs.qv.release();
+    nbufs.partial.release(); nbufs.red.release(); nbufs.status.release();
+    if (nbufs.h_red) cudaFreeHost(nbufs.h_red);
+    if (nbufs.h_int) cudaFreeHost(nbufs.h_int);
+    if (s) cudaStreamDestroy(s);
+  }
+
+  template <typename T>
+  void upload(DBuf<T>& b, const T* src, size_t n) {
+    b.ensure(n ? n : 1);
+    if (n) CK(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+
+  void init(const abd_scene_desc* d, const abd_config* c) {
+    cfg = *c;
+    P.dhat = c->dhat;
+    P.kappa = c->kappa;
+    P.d_sqrt = std::sqrt(c->dhat);
+    P.eps_x = c->eps_x;
+    P.ortho_kappa = c->ortho_kappa;
+    P.ground_offset = c->ground_offset;
+    P.dt = c->dt;
+    P.gravity_y = c->gravity_y;
+    P.mu = c->mu;
+    P.epsv = c->dt * c->evh;
+    P.max_uk = c->max_uk;
+    P.psd = c->psd;
+    P.pt_fric = c->pt_fric;
+    P.ee_fric = c->ee_fric;
+    P.vg_fric = c->vg_fric;
+    P.ground = c->ground;
+    P.pt = c->pt;
+    P.ee = c->ee;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    nb = d->n_bodies;
+    nv = d->vert_off[nb];
+    ne = d->edge_off[nb];
+    nf = d->face_off[nb];
+    std::vector<int> hvb(nv), hev(2 * (size_t)ne), hfv(3 * (size_t)nf), sb(nb), se(nb);
+    std::vector<double> rb(6 * (size_t)nb);
+    for (int b = 0; b < nb; ++b) {
+      for (int v = d->vert_off[b]; v < d->vert_off[b + 1]; ++v) hvb[v] = b;
+      for (int e = d->edge_off[b]; e < d->edge_off[b + 1]; ++e)
+        for (int k = 0; k < 2; ++k) {
+          int lv = d->edges[2 * e + k];
+          if (lv < 0 || lv >= d->vert_off[b + 1] - d->vert_off[b]) throw std::invalid_argument("edge vertex id");
+          hev[2 * e + k] = d->vert_off[b] + lv;
+        }
+      for (int f = d->face_off[b]; f < d->face_off[b + 1]; ++f)
+        for (int k = 0; k < 3; ++k) {
+          int lv = d->faces[3 * f + k];
+          if (lv < 0 || lv >= d->vert_off[b + 1] - d->vert_off[b]) throw std::invalid_argument("face vertex id");
+          hfv[3 * f + k] = d->vert_off[b] + lv;
+        }
+      // rest AABB inflated by sqrt(dhat) (iaabb.cpp:23-39)
+      double lo[3], hi[3];
+      for (int v = d->vert_off[b]; v < d->vert_off[b + 1]; ++v)
+        for (int k = 0; k < 3; ++k) {
+          double x = d->rest_vertices[3 * v + k];
+          if (v == d->vert_off[b]) lo[k] = hi[k] = x;
+          else {
+            lo[k] = x < lo[k] ? x : lo[k];
+            hi[k] = hi[k] < x ? x : hi[k];
+          }
+        }
+      for (int k = 0; k < 3; ++k) {
+        rb[6 * b + k] = lo[k] - P.d_sqrt;
+        rb[6 * b + 3 + k] = hi[k] + P.d_sqrt;
+      }
+    }
+    // scene ranges (bodies of a scene are contiguous)
+    for (int b = 0; b < nb;) {
+      int e = b + 1;
+      if (d->scene_id)
+        while (e < nb && d->scene_id[e] == d->scene_id[b]) ++e;
+      else
+        e = nb;
+      for (int k = b; k < e; ++k) {
+        sb[k] = b;
+        se[k] = e;
+      }
+      b = e;
+    }
+    upload(v_off, d->vert_off, nb + 1);
+    upload(e_off, d->edge_off, nb + 1);
+    upload(f_off, d->face_off, nb + 1);
+    upload(vbody, hvb.data(), nv);
+    upload(ev, hev.data(), 2 * (size_t)ne);
+    upload(fv, hfv.data(), 3 * (size_t)nf);
+    upload(scene_beg, sb.data(), nb);
+    upload(scene_end, se.data(), nb);
+    upload(rest, d->rest_vertices, 3 * (size_t)nv);
+    upload(mass, d->mass, nb);
+    upload(Ic, d->Ic, nb);
+    upload(rest_box, rb.data(), 6 * (size_t)nb);
+    upload(q0, d->q0, 12 * (size_t)nb);
+    upload(q, d->q0, 12 * (size_t)nb);
+    upload(dqdt, d->dqdt, 12 * (size_t)nb);
+    dq.ensure(12 * (size_t)nb);
+    CK(cudaMemsetAsync(dq.p, 0, 12 * (size_t)nb * sizeof(double), s));
+    X.ensure(3 * (size_t)nv + 3);
+    Xq.ensure(3 * (size_t)nv + 3);
+    X0.ensure(3 * (size_t)nv + 3);
+    CK(cudaStreamSynchronize(s));
+  }
+
+  // Algorithmic bytes of the path (per-stage formula, from logged counts).
+  double bytes_cull(const PairSet& S) const {
+    return 48.0 * nv + 24.0 * nv + 20.0 * (S.npt + S.nee + S.nvg);
+  }
+  double bytes_assemble(const PairSet& S) const {
+    double P_ = S.npt + S.nee;
+    return (20 + 96 + 96) * P_ + 200 * P_ + 2 * 1152.0 * (nb + 2.0 * S.nov) + 2 * 96.0 * nb;
+  }
+
+  int step_frame(abd_frame_stats& st) {
+    using clk = std::chrono::steady_clock;
+    auto ms = [](clk::time_point a, clk::time_point b) {
+      return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    Geo g = geo();
+    const int n12 = 12 * nb;
+    launch_copy(q.p, q0.p, n12, s);
+    CK(cudaMemsetAsync(dq.p, 0, n12 * sizeof(double), s));
+    launch_project(g, 0, 0.0, s);
+    double tp, tg;
+    cull(g, P, 1, 0.0, cs, sets[cur], &tp, &tg, s);
+    st.bytes_moved += bytes_cull(sets[cur]);
+    bool term = false;
+    int status = ABD_OK;
+    do {
+      auto t0 = clk::now();
+      PairSet& S = sets[cur];
+      st.n_pt = std::max(st.n_pt, S.npt);
+      st.n_ee = std::max(st.n_ee, S.nee);
+      st.n_vg = std::max(st.n_vg, S.nvg);
+      st.n_overlaps = std::max(st.n_overlaps, S.nov);
+      assemble(g, P, S, nbufs, s);
+      CK(cudaStreamSynchronize(s));
+      st.bytes_moved += bytes_assemble(S);
+      auto t1 = clk::now();
+      int pst = 0;
+      int its = pcg_solve(g, S, nbufs, cfg.pcg_rel_tol, cfg.pcg_max_iter, dq.p, s, &pst);
+      st.pcg_iters += its;
+      st.bytes_moved += its * (1152.0 * (nb + 2.0 * S.nov) + 6 * 96.0 * nb) + 1152.0 * nb;
+      if (pst == ABD_ERR_NOT_SPD) return ABD_ERR_NOT_SPD;
+      if (pst == ABD_ERR_PCG_NOCONV) status = ABD_ERR_PCG_NOCONV;
+      double dd[3];
+      dots(n12, dq.p, nbufs.grad.p, nbufs, dd, s);
+      double sup_dq = std::sqrt(dd[2]);
+      if (std::isnan(sup_dq)) return ABD_ERR_NAN;
+      auto t2 = clk::now();
+      // CCD step bound (abd.cpp:142-196)
+      double toi = 1.0, factor = 1.0;
+      if (cfg.upper_bound) {
+        cull(g, P, 3, 1.0, cs, sets[2], &tp, &tg, s);
+        st.bytes_moved += 96.0 * nv + 20.0 * sets[2].nov;
+        if (cfg.ground) {
+          if (tg < 1e-6) g_cnt++;
+          else g_cnt = 0;
+        }
+        if (tp < 1e-6) p_cnt++;
+        else p_cnt = 0;
+        toi = cfg.ground ? std::min(tg, tp) : tp;
+        if ((cfg.ground && g_cnt > 1) || p_cnt > 1) return ABD_ERR_TOI_TINY;
+      }
+      if (toi < 1.0) factor = cfg.backoff;
+      st.toi_min = std::min(st.toi_min, toi);
+      launch_scale(dq.p, n12, factor * toi, s);
+      auto t3 = clk::now();
+      // line search (line_search.cpp:39-136)
+      double alpha = 1.0;
+      if (cfg.line_search) {
+        launch_project(g, 1, 0.0, s);
+        double E0 = energy(g, P, 0.0, S, S, true, nbufs, s);
+        dots(n12, dq.p, nbufs.grad.p, nbufs, dd, s);
+        double qdg = dd[0], gn = std::sqrt(dd[1]), dqn = std::sqrt(dd[2]);
+        int other = 1 - cur;
+        int trials = 0;
+        bool stalled = true;
+        for (int guard = 0; guard < 2200; ++guard) {
+          cull(g, P, 2, alpha, cs, sets[other], &tp, &tg, s);
+          double E1 = energy(g, P, alpha, sets[other], S, true, nbufs, s);
+          ++trials;
+          st.bytes_moved += bytes_cull(sets[other]) + 48.0 * nv + 116.0 * (sets[other].npt + sets[other].nee);
+          bool wolfe = E1 <= E0 + cfg.c1 * alpha * qdg;
+          alpha /= 2;
+          if (!(!wolfe && gn > cfg.ls_grad_tol)) {
+            stalled = false;
+            break;
+          }
+          if (dqn * alpha * 2 < cfg.tol && cfg.clip) {
+            alpha = 0.0;
+            stalled = false;
+            break;
+          }
+        }
+        st.ls_trials += trials;
+        if (stalled) status = ABD_ERR_LS_STALL;
+        cur = other;
+        alpha *= 2;
+      }
+      st.alpha_min = std::min(st.alpha_min, alpha);
+      launch_q_update(q.p, dq.p, n12, alpha, s);
+      if (!cfg.line_search) launch_project(g, 1, 0.0, s);
+      CK(cudaStreamSynchronize(s));
+      auto t4 = clk::now();
+      st.t_ipc_ms += ms(t0, t1);
+      st.t_solver_ms += ms(t1, t2);
+      st.t_ccd_ms += ms(t2, t3);
+      st.t_ls_ms += ms(t3, t4);
+      st.newton_iters++;
+      term = sup_dq < cfg.tol || ++iter >= cfg.max_iter;
+    } while (!term);
+    ++iter;
+    launch_frame_end(q.p, q0.p, dqdt.p, n12, P.dt, s);
+    CK(cudaStreamSynchronize(s));
+    last_cull_set = cur;
+    return status;
+  }
+};
+
+}  // namespace abd
+
+using abd::Engine;
+
+struct abd_handle {
+  Engine e;
+};
+
+namespace {
+std::string g_last_error;
+
+template <typename F>
+int guarded(abd_handle* h, F&& f) {
+  try {
+    return f();
+  } catch (const abd::CudaError& ce) {
+    std::string m = std::string(ce.where) + ": " + cudaGetErrorString(ce.code);
+    if (h) h->e.err = m;
+    g_last_error = m;
+    return ABD_ERR_CUDA;
+  } catch (const std::invalid_argument& ia) {
+    if (h) h->e.err = ia.what();
+    g_last_error = ia.what();
+    return ABD_ERR_INVALID;
+  } catch (const std::exception& ex) {
+    if (h) h->e.err = ex.what();
+    g_last_error = ex.what();
+    return ABD_ERR_CUDA;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int abd_create(const abd_scene_desc* scene, const abd_config* cfg, abd_handle** out) {
+  if (!scene || !cfg || !out || scene->n_bodies <= 0) return ABD_ERR_INVALID;
+  abd_handle* h = new abd_handle();
+  int rc = guarded(h, [&]() {
+    h->e.init(scene, cfg);
+    return (int)ABD_OK;
+  });
+  if (rc != ABD_OK) {
+    delete h;
+    *out = nullptr;
+    return rc;
+  }
+  *out = h;
+  return ABD_OK;
+}
+
+void abd_destroy(abd_handle* h) { delete h; }
+
+const char* abd_last_error(abd_handle* h) { return h ? h->e.err.c_str() : g_last_error.c_str(); }
+
+int abd_step(abd_handle* h, double dt, int n_frames, abd_frame_stats* stats) {
+  if (!h || n_frames < 0) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    abd_frame_stats st;
+    std::memset(&st, 0, sizeof(st));
+    st.toi_min = 1.0;
+    st.alpha_min = 1.0;
+    if (dt > 0) h->e.P.dt = dt;
+    int rc = ABD_OK;
+    for (int f = 0; f < n_frames; ++f) {
+      rc = h->e.step_frame(st);
+      st.frames++;
+      if (rc != ABD_OK && rc != ABD_ERR_PCG_NOCONV && rc != ABD_ERR_LS_STALL) break;
+    }
+    st.status = rc;
+    if (stats) *stats = st;
+    return rc;
+  });
+}
+
+int abd_get_state(abd_handle* h, double* q0, double* qdot) {
+  if (!h) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    size_t n = 12 * (size_t)h->e.nb * sizeof(double);
+    if (q0) CK(cudaMemcpyAsync(q0, h->e.q0.p, n, cudaMemcpyDeviceToHost, h->e.s));
+    if (qdot) CK(cudaMemcpyAsync(qdot, h->e.dqdt.p, n, cudaMemcpyDeviceToHost, h->e.s));
+    CK(cudaStreamSynchronize(h->e.s));
+    return (int)ABD_OK;
+  });
+}
+
+int abd_set_state(abd_handle* h, const double* q0, const double* qdot) {
+  if (!h) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    size_t n = 12 * (size_t)h->e.nb * sizeof(double);
+    if (q0) {
+      CK(cudaMemcpyAsync(h->e.q0.p, q0, n, cudaMemcpyHostToDevice, h->e.s));
+      CK(cudaMemcpyAsync(h->e.q.p, q0, n, cudaMemcpyHostToDevice, h->e.s));
+    }
+    if (qdot) CK(cudaMemcpyAsync(h->e.dqdt.p, qdot, n, cudaMemcpyHostToDevice, h->e.s));
+    CK(cudaStreamSynchronize(h->e.s));
+    return (int)ABD_OK;
+  });
+}
+
+int abd_get_counts(abd_handle* h, int* n_bodies, int* n_vertices, int* n_edges, int* n_faces) {
+  if (!h) return ABD_ERR_INVALID;
+  if (n_bodies) *n_bodies = h->e.nb;
+  if (n_vertices) *n_vertices = h->e.nv;
+  if (n_edges) *n_edges = h->e.ne;
+  if (n_faces) *n_faces = h->e.nf;
+  return ABD_OK;
+}
+
+int abd_get_iter(abd_handle* h) { return h ? h->e.iter : -1; }
+int abd_set_iter(abd_handle* h, int it) {
+  if (!h) return ABD_ERR_INVALID;
+  h->e.iter = it;
+  return ABD_OK;
+}
+
+int abd_cull(abd_handle* h, int vtn, const double* q, const double* dq, int* counts, double* toi) {
+  if (!h || !q || vtn < 1 || vtn > 3) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    Engine& e = h->e;
+    size_t n = 12 * (size_t)e.nb;
+    CK(cudaMemcpyAsync(e.q.p, q, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
+    if (dq) CK(cudaMemcpyAsync(e.dq.p, dq, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
+    else CK(cudaMemsetAsync(e.dq.p, 0, n * sizeof(double), e.s));
+    double tp = 1.0, tg = 1.0;
+    abd::Geo g = e.geo();
+    abd::PairSet& S = e.sets[e.cur];
+    abd::cull(g, e.P, vtn, 1.0, e.cs, vtn == 3 ? e.sets[2] : S, &tp, &tg, e.s);
+    CK(cudaStreamSynchronize(e.s));
+    if (vtn == 3) {
+      if (toi) *toi = e.cfg.ground ? std::min(tp, tg) : tp;
+      if (counts) counts[3] = e.sets[2].nov;
+    } else {
+      e.last_cull_set = e.cur;
+      if (counts) {
+        counts[0] = S.npt;
+        counts[1] = S.nee;
+        counts[2] = S.nvg;
+        counts[3] = S.nov;
+      }
+    }
+    return (int)ABD_OK;
+  });
+}
+
+int abd_get_pairs(abd_handle* h, int* pt, int* pt_type, int* ee, int* ee_type, int* vg) {
+  if (!h) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    Engine& e = h->e;
+    CK(cudaStreamSynchronize(e.s));
+    abd::PairSet& S = e.sets[e.last_cull_set];
+    std::vector<int8_t> t8(std::max(S.npt, S.nee) + 1);
+    if (pt && S.npt) CK(cudaMemcpy(pt, S.pt.p, 4 * (size_t)S.npt * sizeof(int), cudaMemcpyDeviceToHost));
+    if (pt_type && S.npt) {
+      CK(cudaMemcpy(t8.data(), S.pt_ty.p, S.npt, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < S.npt; ++i) pt_type[i] = t8[i];
+    }
+    if (ee && S.nee) CK(cudaMemcpy(ee, S.ee.p, 4 * (size_t)S.nee * sizeof(int), cudaMemcpyDeviceToHost));
+    if (ee_type && S.nee) {
+      CK(cudaMemcpy(t8.data(), S.ee_ty.p, S.nee, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < S.nee; ++i) ee_type[i] = t8[i];
+    }
+    if (vg && S.nvg) CK(cudaMemcpy(vg, S.vg.p, 2 * (size_t)S.nvg * sizeof(int), cudaMemcpyDeviceToHost));
+    return (int)ABD_OK;
+  });
+}
+
+static int newton_system_at(Engine& e, const double* q) {
+  size_t n = 12 * (size_t)e.nb;
+  CK(cudaMemcpyAsync(e.q.p, q, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
+  CK(cudaMemsetAsync(e.dq.p, 0, n * sizeof(double), e.s));
+  abd::Geo g = e.geo();
+  abd::launch_project(g, 0, 0.0, e.s);
+  double tp, tg;
+  abd::cull(g, e.P, 1, 0.0, e.cs, e.sets[e.cur], &tp, &tg, e.s);
+  abd::assemble(g, e.P, e.sets[e.cur], e.nbufs, e.s);
+  CK(cudaStreamSynchronize(e.s));
+  e.last_cull_set = e.cur;
+  return ABD_OK;
+}
+
+int abd_newton_system(abd_handle* h, const double* q, double* grad, double* diag, int* n_off, int* off_keys,
+                      double* off_vals, int max_off) {
+  if (!h || !q) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    Engine& e = h->e;
+    newton_system_at(e, q);
+    abd::PairSet& S = e.sets[e.cur];
+    if (grad) CK(cudaMemcpy(grad, e.nbufs.grad.p, 12 * (size_t)e.nb * sizeof(double), cudaMemcpyDeviceToHost));
+    if (diag) CK(cudaMemcpy(diag, e.nbufs.D.p, 144 * (size_t)e.nb * sizeof(double), cudaMemcpyDeviceToHost));
+    int nov = S.nov;
+    std::vector<int> has(nov + 1), oi(nov + 1), oj(nov + 1);
+    if (nov) {
+      CK(cudaMemcpy(has.data(), e.nbufs.has.p, nov * sizeof(int), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(oi.data(), S.ovI.p, nov * sizeof(int), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(oj.data(), S.ovJ.p, nov * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    int k = 0;
+    for (int u = 0; u < nov; ++u) {
+      if (!has[u]) continue;
+      if (off_keys && k < max_off) {
+        off_keys[2 * k] = oi[u];
+        off_keys[2 * k + 1] = oj[u];
+        CK(cudaMemcpy(off_vals + 144 * (size_t)k, e.nbufs.ovr.p + (size_t)u * abd::CONTRIB + 288,
+                      144 * sizeof(double), cudaMemcpyDeviceToHost));
+      }
+      ++k;
+    }
+    if (n_off) *n_off = k;
+    return (int)ABD_OK;
+  });
+}
+
+int abd_newton_dq(abd_handle* h, const double* q, double* dq, int* pcg_iters) {
+  if (!h || !q || !dq) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    Engine& e = h->e;
+    newton_system_at(e, q);
+    int st = 0;
+    int its = abd::pcg_solve(e.geo(), e.sets[e.cur], e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.dq.p, e.s, &st);
+    if (pcg_iters) *pcg_iters = its;
+    CK(cudaMemcpy(dq, e.dq.p, 12 * (size_t)e.nb * sizeof(double), cudaMemcpyDeviceToHost));
+    return st;
+  });
+}
+
+}  // extern "C"

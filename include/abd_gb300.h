@@ -1,0 +1,142 @@
+/*
+ * abd_gb300 — C ABI of the GB300 affine-body contact step.
+ *
+ * One handle owns one (possibly batched) scene resident in GPU memory and advances it
+ * one frame at a time with the reference's per-frame step (ABD::implicit_euler,
+ * model/abd.cpp:30-140): iAABB culling into point-triangle / edge-edge / vertex-ground
+ * pair sets, IPC barrier + lagged friction terms projected to PSD, the 12x12
+ * block-sparse Newton system, a block-Jacobi PCG solve, the CCD step bound and the
+ * Armijo line search. Every call returns an abd_status; nothing exits the process.
+ *
+ * Plain pointers and sizes only; all host arrays are owned by the caller and copied.
+ * One thread per handle; handles are independent. Body state layout per body:
+ * 12 doubles q = [p(3), a1(3), a2(3), a3(3)], a_k the columns of A (x = A xbar + p),
+ * the same order as the reference's `cat(c.q)` (model/mutils.cpp:44-51) and its trace
+ * files (player_save, model/mutils.cpp:293-329).
+ */
+#ifndef ABD_GB300_H
+#define ABD_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  ABD_OK = 0,
+  ABD_ERR_NAN = 1,            /* non-finite Newton step (reference: exit(1), abd.cpp:288-291) */
+  ABD_ERR_LS_STALL = 2,       /* line search hit its trial cap (reference: unbounded loop) */
+  ABD_ERR_PAIR_OVERFLOW = 3,  /* a pair buffer could not be grown */
+  ABD_ERR_TOI_TINY = 4,       /* TOI < 1e-6 twice in a row (reference: exit(1), iaabb.cpp:306-313) */
+  ABD_ERR_NOT_SPD = 5,        /* a diagonal block was not positive definite */
+  ABD_ERR_PCG_NOCONV = 6,     /* PCG hit its iteration cap (the step is still taken) */
+  ABD_ERR_CUDA = 7,           /* CUDA runtime error; see abd_last_error */
+  ABD_ERR_INVALID = 8,        /* invalid argument */
+  ABD_ERR_IO = 9              /* config / scene / mesh file could not be read */
+} abd_status;
+
+/* Step parameters. Field names follow the reference's config.json keys
+ * (view/control.cpp:19-111); dhat, ortho_kappa and ground_offset are the values the
+ * reference hard-codes (barrier.cpp:7-8, othogonal_energy.cpp:8, geometry.cpp:60). */
+typedef struct {
+  double dt;
+  double kappa;          /* barrier stiffness ("kappa") */
+  double dhat;           /* squared-distance activation distance */
+  double ortho_kappa;    /* orthogonality stiffness */
+  double ground_offset;  /* vertex-ground distance is y + ground_offset (0.5) */
+  double mu;             /* friction coefficient */
+  double evh;            /* friction epsilon_v * h = dt * evh */
+  double eps_x;          /* edge-edge mollifier scale */
+  double backoff;        /* CCD backoff factor */
+  double c1;             /* Armijo constant (params_double.c1) */
+  double tol;            /* Newton tolerance on |dq| (params_double.tol) */
+  double max_uk;         /* params_double.max_uk */
+  double gravity_y;      /* -9.8 with "gravity": true */
+  double ls_grad_tol;    /* line search stops when |grad| <= this (1e-3 in the reference) */
+  double pcg_rel_tol;    /* PCG relative residual target */
+  int max_iter;          /* cumulative Newton cap, as the reference's `iter` member */
+  int ground, pt, ee, psd, line_search, upper_bound;
+  int vg_fric, pt_fric, ee_fric, clip;
+  int pcg_max_iter;
+} abd_config;
+
+/* Scene: bodies with their rest meshes (local vertex ids per body). */
+typedef struct {
+  int n_bodies;
+  const double* q0;            /* n_bodies * 12 */
+  const double* dqdt;          /* n_bodies * 12 */
+  const double* mass;          /* n_bodies; < 0 marks a static body */
+  const double* Ic;            /* n_bodies */
+  const int* vert_off;         /* n_bodies + 1 */
+  const double* rest_vertices; /* vert_off[n] * 3 */
+  const int* edge_off;         /* n_bodies + 1 */
+  const int* edges;            /* edge_off[n] * 2, local vertex ids */
+  const int* face_off;         /* n_bodies + 1 */
+  const int* faces;            /* face_off[n] * 3, local vertex ids */
+  const int* scene_id;         /* n_bodies or NULL: bodies of different scenes never touch;
+                                  bodies of one scene must be contiguous */
+} abd_scene_desc;
+
+typedef struct {
+  int frames, newton_iters, ls_trials, pcg_iters;
+  int n_pt, n_ee, n_vg, n_overlaps; /* maxima over the frames */
+  int status;
+  int pad;
+  double toi_min, alpha_min;
+  double t_ipc_ms, t_solver_ms, t_ccd_ms, t_ls_ms; /* reference's 4-phase breakdown */
+  double bytes_moved;                               /* algorithmic bytes of the path */
+} abd_frame_stats;
+
+typedef struct abd_handle abd_handle;
+
+/* Replaces ABD(cubes, globals) (model/abd.h:13-14). */
+int abd_create(const abd_scene_desc* scene, const abd_config* cfg, abd_handle** out);
+/* Reads a reference config.json and scene JSON (test_cases/spinning_cube.cpp:56-127;
+ * "obj" meshes resolved relative to the scene file). */
+int abd_create_from_files(const char* config_json, const char* scene_json, abd_handle** out);
+/* Replaces ABD::implicit_euler(dt) (model/abd.cpp:30): advances n_frames frames. */
+int abd_step(abd_handle* h, double dt, int n_frames, abd_frame_stats* stats);
+int abd_get_state(abd_handle* h, double* q0, double* qdot);
+int abd_set_state(abd_handle* h, const double* q0, const double* qdot);
+int abd_get_counts(abd_handle* h, int* n_bodies, int* n_vertices, int* n_edges, int* n_faces);
+/* Cumulative Newton counter (the reference's ABD::iter, model/abd.h:53). */
+int abd_get_iter(abd_handle* h);
+int abd_set_iter(abd_handle* h, int iter);
+const char* abd_last_error(abd_handle* h);
+void abd_destroy(abd_handle* h);
+
+/* ---- stage entry points (parity tests and profiling) ---- */
+/* Culls at state q (+ dq): vtn 1 at q, 2 at q + dq, 3 the trajectory q -> q + dq.
+ * counts[0..3] = pt, ee, vg pairs, overlaps; *toi is written for vtn 3. */
+int abd_cull(abd_handle* h, int vtn, const double* q, const double* dq, int* counts, double* toi);
+/* Pair set of the last vtn 1/2 cull: pt/ee tuples (body, prim, body, prim), types. */
+int abd_get_pairs(abd_handle* h, int* pt, int* pt_type, int* ee, int* ee_type, int* vg);
+/* Newton system at state q for the pair set culled at q: gradient (12 nb), diagonal
+ * blocks (144 nb, row-major), upper off-diagonal blocks (keys I<J, 144 each). */
+int abd_newton_system(abd_handle* h, const double* q, double* grad, double* diag, int* n_off, int* off_keys,
+                      double* off_vals, int max_off);
+/* Newton step dq = -H^{-1} grad at state q (PCG). */
+int abd_newton_dq(abd_handle* h, const double* q, double* dq, int* pcg_iters);
+
+/* ---- per-primitive functions (the reference's python `abdtk` module,
+ *      python/bindings.cpp:42-83), batched over n primitives ---- */
+/* x: n * 12 (p, t0, t1, t2). type / dist optional (computed when type[i] < 0).
+ * H: n * 144 row-major vertex-space Hessian, g: n * 12. */
+int abd_ipc_hess_pt_batch(int n, const double* x, const int* type, const double* dist, double dhat, double kappa,
+                          int psd, double* H, double* g);
+int abd_ipc_hess_ee_batch(int n, const double* x, const int* type, const double* dist, double dhat, double kappa,
+                          double eps_x, int psd, double* H, double* g, double* mollifier);
+/* x: n * 24 (four points at t0 then four at t1). */
+int abd_pt_collision_time_batch(int n, const double* x, double* toi);
+int abd_ee_collision_time_batch(int n, const double* x, double* toi);
+/* Distance type and squared distance; x: n * 12. */
+int abd_pt_distance_batch(int n, const double* x, int* type, double* dist);
+int abd_ee_distance_batch(int n, const double* x, int* type, double* dist);
+
+/* Dense FP64 FMA throughput of this GPU in GFLOP/s (roofline denominator for the
+ * FP64-bound kernels; measured with a fixed independent-FMA kernel). */
+double abd_measure_fp64_gflops(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ABD_GB300_H */
