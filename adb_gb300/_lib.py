@@ -35,9 +35,9 @@ class AbdSceneDesc(C.Structure):
 
 class AbdFrameStats(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("frames", "newton_iters", "ls_trials", "pcg_iters", "n_pt", "n_ee", "n_vg",
-                                       "n_overlaps", "status", "pad")] + [
+                                       "n_overlaps", "status", "pad")] + [("kernel_launches", C.c_longlong)] + [
         (n, C.c_double) for n in ("toi_min", "alpha_min", "t_ipc_ms", "t_solver_ms", "t_ccd_ms", "t_ls_ms",
-                                  "bytes_moved")]
+                                  "bytes_moved", "device_ms")]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_ if f[0] != "pad"}
@@ -79,6 +79,9 @@ def lib():
         L.abd_ee_collision_time_batch.argtypes = [C.c_int, _D, _D]
         L.abd_pt_distance_batch.argtypes = [C.c_int, _D, _I, _D]
         L.abd_ee_distance_batch.argtypes = [C.c_int, _D, _I, _D]
+        L.abd_profile.argtypes = [H, C.c_int]
+        L.abd_kernel_times.argtypes = [H, C.c_int, C.c_char_p, _D, C.POINTER(C.c_longlong)]
+        L.abd_kernel_work.argtypes = [H, C.c_int, C.c_char_p, _D, C.POINTER(C.c_longlong), _D, _D]
         L.abd_measure_fp64_gflops.restype = C.c_double
         L.abd_measure_fp64_gflops.argtypes = []
         _lib = L
@@ -87,7 +90,7 @@ def lib():
 
 # Every symbol include/abd_gb300.h declares (checked by the CPU test suite).
 EXPORTED = ["abd_create", "abd_create_from_files", "abd_step", "abd_get_state", "abd_set_state", "abd_get_counts",
-            "abd_get_iter", "abd_set_iter", "abd_last_error", "abd_destroy", "abd_cull", "abd_get_pairs",
+            "abd_get_iter", "abd_set_iter", "abd_last_error", "abd_destroy", "abd_profile", "abd_kernel_times", "abd_kernel_work", "abd_cull", "abd_get_pairs",
             "abd_newton_system", "abd_newton_dq", "abd_ipc_hess_pt_batch", "abd_ipc_hess_ee_batch",
             "abd_pt_collision_time_batch", "abd_ee_collision_time_batch", "abd_pt_distance_batch",
             "abd_ee_distance_batch", "abd_measure_fp64_gflops"]

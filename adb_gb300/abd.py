@@ -111,6 +111,25 @@ class ABD:
     def iter(self, v: int):
         L.lib().abd_set_iter(self._h, int(v))
 
+    # --- per-kernel device timing -----------------------------------------------------
+    def profile(self, enable: bool = True):
+        L.check(L.lib().abd_profile(self._h, int(enable)), self._h, "abd_profile")
+
+    def kernel_times(self):
+        """{kernel class: dict(ms, launches, units, bytes)} since the last profile() call."""
+        n = 64
+        names = C.create_string_buffer(32 * n)
+        ms, units, byts = np.zeros(n), np.zeros(n), np.zeros(n)
+        cnt = np.zeros(n, np.int64)
+        k = L.lib().abd_kernel_work(self._h, n, names, L.dptr(ms), cnt.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                    L.dptr(units), L.dptr(byts))
+        out = {}
+        for i in range(k):
+            nm = names.raw[32 * i: 32 * i + 32].split(b"\0")[0].decode()
+            out[nm] = {"ms": float(ms[i]), "launches": int(cnt[i]), "units": float(units[i]),
+                       "bytes": float(byts[i])}
+        return out
+
     # --- stage access (parity tests, profiling) ------------------------------------
     def cull(self, vtn: int, q: np.ndarray, dq: Optional[np.ndarray] = None):
         q = np.ascontiguousarray(q, np.float64)

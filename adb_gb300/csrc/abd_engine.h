@@ -99,6 +99,52 @@ struct CullScratch {
   unsigned long long* h_toi = nullptr;
 };
 
+// ---------------- launch accounting ----------------
+// Every kernel launch of the step goes through KLAUNCH: it counts the launch and, when
+// profiling is on, brackets it with CUDA events on its stream so that each kernel's
+// device time is measured live.
+enum KTag {
+  K_PROJECT, K_BODY_BOXES, K_OV_COUNT, K_OV_FILL, K_OV_LOWER, K_PRIM_BOXES, K_BIN, K_CAND_COUNT, K_NARROW_FLAGS,
+  K_NARROW_WRITE, K_NARROW_TOI, K_VG, K_VG_TOI, K_SCAN, K_PAIR_TERMS, K_SEG, K_OV_REDUCE, K_BODY_SYSTEM,
+  K_BLOCK_INVERSE, K_PCG, K_ENERGY, K_DOTS, K_VEC, K_NTAGS
+};
+extern const char* const kTagNames[K_NTAGS];
+struct Prof {
+  bool on = false;
+  long long launches = 0;
+  double ms[K_NTAGS] = {};
+  double bytes[K_NTAGS] = {};   // algorithmic bytes of the launches (per-unit figure x units)
+  double units[K_NTAGS] = {};   // work units of the launches (pairs, candidates, rows, ...)
+  long long cnt[K_NTAGS] = {};
+  struct Rec {
+    int tag;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> pend;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get();
+  void begin(int tag, cudaStream_t s, cudaEvent_t& a);
+  void end(int tag, cudaStream_t s, cudaEvent_t a);
+  void flush();  // after a stream synchronisation
+  void reset();
+  ~Prof();
+};
+extern thread_local Prof* g_prof;
+inline void prof_work(int tag, double units, double bytes) {
+  if (g_prof) {
+    g_prof->units[tag] += units;
+    g_prof->bytes[tag] += bytes;
+  }
+}
+#define KLAUNCH(tag, stream, ...)                            \
+  do {                                                      \
+    cudaEvent_t _ka = nullptr;                              \
+    if (::abd::g_prof) ::abd::g_prof->begin((tag), (stream), _ka); \
+    __VA_ARGS__;                                            \
+    CK(cudaGetLastError());                                 \
+    if (::abd::g_prof) ::abd::g_prof->end((tag), (stream), _ka);   \
+  } while (0)
+
 // ---------------- scan ----------------
 void scan_exclusive_int(const int* in, int* out, int n, int* d_total, cudaStream_t s, DBuf<int>& tmp);
 void scan_exclusive_ll(const long long* in, long long* out, int n, long long* d_total, cudaStream_t s,

@@ -549,8 +549,8 @@ double key_to_double(unsigned long long k) {
 
 void launch_project(const Geo& g, int which, double alpha, cudaStream_t s) {
   if (g.nv == 0) return;
-  k_project<<<nblk(g.nv, 256), 256, 0, s>>>(g, which, alpha);
-  CK(cudaGetLastError());
+  KLAUNCH(K_PROJECT, s, k_project<<<nblk(g.nv, 256), 256, 0, s>>>(g, which, alpha));
+  prof_work(K_PROJECT, g.nv, 48.0 * g.nv);  // rest read + world write per vertex
 }
 
 void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs, PairSet& out, double* toi_p,
@@ -575,10 +575,8 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
   cs.up_ptr.ensure(nb + 1);
   PairSet& S = out;
   S.row_ptr.ensure(nb + 1);
-  k_body_boxes<<<nblk(nb, 128), 128, 0, s>>>(g, vtn, alpha, cs.bbox.p);
-  CK(cudaGetLastError());
-  k_ov_count<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, cs.cnt_all.p, cs.cnt_up.p);
-  CK(cudaGetLastError());
+  KLAUNCH(K_BODY_BOXES, s, k_body_boxes<<<nblk(nb, 128), 128, 0, s>>>(g, vtn, alpha, cs.bbox.p));
+  KLAUNCH(K_OV_COUNT, s, k_ov_count<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, cs.cnt_all.p, cs.cnt_up.p));
   cs.tmp_int.ensure(64);
   int* d_tot = cs.tmp_int.p;  // [0] nnz, [1] nov
   scan_exclusive_int(cs.cnt_all.p, S.row_ptr.p, nb, d_tot, s, cs.vflag_cnt);
@@ -596,35 +594,30 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
   S.ovJ.ensure(nov + 1);
   cs.ovcull.ensure(6 * (size_t)nov + 6);
   cs.ovcull_f.ensure(6 * (size_t)nov + 6);
-  k_ov_fill<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, S.row_ptr.p, cs.up_ptr.p, S.col.p,
+  KLAUNCH(K_OV_FILL, s, k_ov_fill<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, S.row_ptr.p, cs.up_ptr.p, S.col.p,
                                                           cs.rowid.p, S.upidx.p, S.ovI.p, S.ovJ.p, cs.ovcull.p,
-                                                          cs.ovcull_f.p);
-  CK(cudaGetLastError());
+                                                          cs.ovcull_f.p));
   if (nnz) {
-    k_ov_lower<<<nblk(nnz, 256), 256, 0, s>>>(nnz, S.row_ptr.p, S.col.p, cs.rowid.p, S.upidx.p);
-    CK(cudaGetLastError());
+    KLAUNCH(K_OV_LOWER, s, k_ov_lower<<<nblk(nnz, 256), 256, 0, s>>>(nnz, S.row_ptr.p, S.col.p, cs.rowid.p, S.upidx.p));
   }
   // 4. primitive boxes and binning
   cs.vbox.ensure(6 * (size_t)g.nv + 6);
   cs.ebox.ensure(6 * (size_t)g.ne + 6);
   cs.fbox.ensure(6 * (size_t)g.nf + 6);
   long long nprim = (long long)g.nv + g.ne + g.nf;
-  k_prim_boxes<<<nblk(nprim, 256), 256, 0, s>>>(g, traj, cs.vbox.p, cs.ebox.p, cs.fbox.p);
-  CK(cudaGetLastError());
+  KLAUNCH(K_PRIM_BOXES, s, k_prim_boxes<<<nblk(nprim, 256), 256, 0, s>>>(g, traj, cs.vbox.p, cs.ebox.p, cs.fbox.p));
   long long total = 0;
   if (nov > 0) {
     cs.bin_cnt.ensure(6 * (size_t)nov + 6);
     cs.bin_off.ensure(6 * (size_t)nov + 6);
     int nw = 2 * nov;
-    k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, 0, traj, S.ovI.p, S.ovJ.p, cs.ovcull.p,
+    KLAUNCH(K_BIN, s, k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, 0, traj, S.ovI.p, S.ovJ.p, cs.ovcull.p,
                                                         cs.ovcull_f.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.bin_cnt.p,
-                                                        nullptr, nullptr);
-    CK(cudaGetLastError());
+                                                        nullptr, nullptr));
     scan_exclusive_int(cs.bin_cnt.p, cs.bin_off.p, 6 * nov, d_tot + 2, s, cs.vflag_cnt);
     cs.cand_cnt.ensure(nov + 1);
     cs.cand_off.ensure(nov + 2);
-    k_cand_count<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.bin_cnt.p, cs.cand_cnt.p);
-    CK(cudaGetLastError());
+    KLAUNCH(K_CAND_COUNT, s, k_cand_count<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.bin_cnt.p, cs.cand_cnt.p));
     scan_exclusive_ll(cs.cand_cnt.p, cs.cand_off.p, nov, cs.cand_off.p + nov, s, cs.tmp_ll);
     CK(cudaMemcpyAsync(cs.h_small + 2, d_tot + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(cs.h_ll, cs.cand_off.p + nov, sizeof(long long), cudaMemcpyDeviceToHost, s));
@@ -632,10 +625,9 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     int nlst = cs.h_small[2];
     total = cs.h_ll[0];
     cs.lst.ensure((size_t)nlst + 1);
-    k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, 1, traj, S.ovI.p, S.ovJ.p, cs.ovcull.p,
+    KLAUNCH(K_BIN, s, k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, 1, traj, S.ovI.p, S.ovJ.p, cs.ovcull.p,
                                                         cs.ovcull_f.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.bin_cnt.p,
-                                                        cs.bin_off.p, cs.lst.p);
-    CK(cudaGetLastError());
+                                                        cs.bin_off.p, cs.lst.p));
   }
   float ds_f = float_round_up(P.d_sqrt);
   int ntile = (int)((total + NTILE - 1) / NTILE);
@@ -648,13 +640,12 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     one[0] = one[1] = b | 0x8000000000000000ull;
     CK(cudaMemcpyAsync(cs.toi_key.p, one, sizeof(one), cudaMemcpyHostToDevice, s));
     if (total > 0) {
-      k_narrow_toi<<<ntile, NT, 0, s>>>(g, nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p, S.ovI.p,
-                                        S.ovJ.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.toi_key.p);
-      CK(cudaGetLastError());
+      prof_work(K_NARROW_TOI, (double)total, 48.0 * g.nv);  // positions at q and q + dq
+      KLAUNCH(K_NARROW_TOI, s, k_narrow_toi<<<ntile, NT, 0, s>>>(g, nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p, S.ovI.p,
+                                        S.ovJ.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.toi_key.p));
     }
     if (P.ground && g.nv) {
-      k_vg_toi<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, cs.toi_key.p + 1);
-      CK(cudaGetLastError());
+      KLAUNCH(K_VG_TOI, s, k_vg_toi<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, cs.toi_key.p + 1));
     }
     CK(cudaMemcpyAsync(cs.h_toi, cs.toi_key.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -670,26 +661,25 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     cs.blk_b.ensure(ntile + 1);
     cs.blk_a_off.ensure(ntile + 1);
     cs.blk_b_off.ensure(ntile + 1);
-    k_narrow_flags<<<ntile, NT, 0, s>>>(g, P, ds_f, nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p,
+    KLAUNCH(K_NARROW_FLAGS, s, k_narrow_flags<<<ntile, NT, 0, s>>>(g, P, ds_f, nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p,
                                         S.ovI.p, S.ovJ.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.flags.p, cs.blk_a.p,
-                                        cs.blk_b.p);
-    CK(cudaGetLastError());
+                                        cs.blk_b.p));
     scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, ntile, d_tot + 3, s, cs.vflag_cnt);
     scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, ntile, d_tot + 4, s, cs.vflag_cnt);
     CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     npt = cs.h_small[3];
     nee = cs.h_small[4];
+    prof_work(K_NARROW_FLAGS, (double)total, 24.0 * g.nv + 20.0 * ((double)npt + nee));
     S.pt.ensure(4 * (size_t)npt + 4);
     S.pt_ty.ensure(npt + 1);
     S.pt_ov.ensure(npt + 1);
     S.ee.ensure(4 * (size_t)nee + 4);
     S.ee_ty.ensure(nee + 1);
     S.ee_ov.ensure(nee + 1);
-    k_narrow_write<<<ntile, NT, 0, s>>>(nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p, S.ovI.p,
+    KLAUNCH(K_NARROW_WRITE, s, k_narrow_write<<<ntile, NT, 0, s>>>(nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p, S.ovI.p,
                                         S.ovJ.p, cs.flags.p, cs.blk_a_off.p, cs.blk_b_off.p, S.pt.p, S.pt_ty.p,
-                                        S.pt_ov.p, S.ee.p, S.ee_ty.p, S.ee_ov.p);
-    CK(cudaGetLastError());
+                                        S.pt_ov.p, S.ee.p, S.ee_ty.p, S.ee_ov.p));
   }
   S.npt = npt;
   S.nee = nee;
@@ -700,19 +690,16 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     int nbv = nblk(g.nv, 256);
     cs.vflag_off.ensure(nbv + 1);
     cs.blk_a.ensure(nbv + 1);
-    k_vg_count<<<nbv, 256, 0, s>>>(g, P, cs.blk_a.p);
-    CK(cudaGetLastError());
+    KLAUNCH(K_VG, s, k_vg_count<<<nbv, 256, 0, s>>>(g, P, cs.blk_a.p));
     scan_exclusive_int(cs.blk_a.p, cs.vflag_off.p, nbv, d_tot + 5, s, cs.vflag_cnt);
     CK(cudaMemcpyAsync(cs.h_small + 5, d_tot + 5, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     nvg = cs.h_small[5];
     S.vg.ensure(2 * (size_t)nvg + 2);
-    k_vg_write<<<nbv, 256, 0, s>>>(g, P, cs.vflag_off.p, S.vg.p);
-    CK(cudaGetLastError());
+    KLAUNCH(K_VG, s, k_vg_write<<<nbv, 256, 0, s>>>(g, P, cs.vflag_off.p, S.vg.p));
   }
   S.nvg = nvg;
-  k_vg_seg<<<nblk(nb + 1, 256), 256, 0, s>>>(nb, nvg, S.vg.p, S.vg_seg.p);
-  CK(cudaGetLastError());
+  KLAUNCH(K_VG, s, k_vg_seg<<<nblk(nb + 1, 256), 256, 0, s>>>(nb, nvg, S.vg.p, S.vg_seg.p));
 }
 
 }  // namespace abd

@@ -16,6 +16,65 @@ void check(cudaError_t e, const char* where) {
   if (e != cudaSuccess) throw CudaError{e, where};
 }
 
+const char* const kTagNames[K_NTAGS] = {
+    "project", "body_boxes", "ov_count", "ov_fill", "ov_lower", "prim_boxes", "bin", "cand_count", "narrow_flags",
+    "narrow_write", "narrow_toi", "vg", "vg_toi", "scan", "pair_terms", "seg", "ov_reduce", "body_system",
+    "block_inverse", "pcg", "energy", "dots", "vec"};
+thread_local Prof* g_prof = nullptr;
+
+cudaEvent_t Prof::get() {
+  if (!pool.empty()) {
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  CK(cudaEventCreate(&e));
+  return e;
+}
+void Prof::begin(int tag, cudaStream_t s, cudaEvent_t& a) {
+  (void)tag;
+  ++launches;
+  if (!on) return;
+  a = get();
+  CK(cudaEventRecord(a, s));
+}
+void Prof::end(int tag, cudaStream_t s, cudaEvent_t a) {
+  if (!on || !a) return;
+  cudaEvent_t b = get();
+  CK(cudaEventRecord(b, s));
+  pend.push_back(Rec{tag, a, b});
+}
+void Prof::flush() {
+  for (auto& r : pend) {
+    CK(cudaEventSynchronize(r.b));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, r.a, r.b));
+    ms[r.tag] += t;
+    cnt[r.tag] += 1;
+    pool.push_back(r.a);
+    pool.push_back(r.b);
+  }
+  pend.clear();
+}
+void Prof::reset() {
+  flush();
+  for (int i = 0; i < K_NTAGS; ++i) {
+    ms[i] = 0;
+    cnt[i] = 0;
+    bytes[i] = 0;
+    units[i] = 0;
+  }
+  launches = 0;
+}
+Prof::~Prof() {
+  for (auto& r : pend) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : pool) cudaEventDestroy(e);
+}
+
 struct Engine {
   abd_config cfg;
   Params P;
@@ -30,6 +89,7 @@ struct Engine {
   int iter = 0, g_cnt = 0, p_cnt = 0;
   int last_cull_set = 0;
   std::string err;
+  Prof prof;
 
   Geo geo() const {
     Geo g;
@@ -296,8 +356,15 @@ struct abd_handle {
 namespace {
 std::string g_last_error;
 
+struct ProfScope {
+  abd::Prof* prev;
+  explicit ProfScope(abd_handle* h) : prev(abd::g_prof) { abd::g_prof = h ? &h->e.prof : nullptr; }
+  ~ProfScope() { abd::g_prof = prev; }
+};
+
 template <typename F>
 int guarded(abd_handle* h, F&& f) {
+  ProfScope ps(h);
   try {
     return f();
   } catch (const abd::CudaError& ce) {
@@ -347,6 +414,11 @@ int abd_step(abd_handle* h, double dt, int n_frames, abd_frame_stats* stats) {
     st.toi_min = 1.0;
     st.alpha_min = 1.0;
     if (dt > 0) h->e.P.dt = dt;
+    long long launches0 = h->e.prof.launches;
+    cudaEvent_t ev0, ev1;
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+    CK(cudaEventRecord(ev0, h->e.s));
     int rc = ABD_OK;
     for (int f = 0; f < n_frames; ++f) {
       rc = h->e.step_frame(st);
@@ -354,6 +426,15 @@ int abd_step(abd_handle* h, double dt, int n_frames, abd_frame_stats* stats) {
       if (rc != ABD_OK && rc != ABD_ERR_PCG_NOCONV && rc != ABD_ERR_LS_STALL) break;
     }
     st.status = rc;
+    CK(cudaEventRecord(ev1, h->e.s));
+    CK(cudaEventSynchronize(ev1));
+    float dms = 0;
+    CK(cudaEventElapsedTime(&dms, ev0, ev1));
+    st.device_ms = dms;
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    h->e.prof.flush();
+    st.kernel_launches = h->e.prof.launches - launches0;
     if (stats) *stats = st;
     return rc;
   });
@@ -394,6 +475,38 @@ int abd_get_counts(abd_handle* h, int* n_bodies, int* n_vertices, int* n_edges, 
 }
 
 int abd_get_iter(abd_handle* h) { return h ? h->e.iter : -1; }
+
+int abd_profile(abd_handle* h, int enable) {
+  if (!h) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    h->e.prof.reset();
+    h->e.prof.on = enable != 0;
+    return (int)ABD_OK;
+  });
+}
+
+int abd_kernel_times(abd_handle* h, int max_n, char* names, double* total_ms, long long* launches) {
+  return abd_kernel_work(h, max_n, names, total_ms, launches, nullptr, nullptr);
+}
+
+int abd_kernel_work(abd_handle* h, int max_n, char* names, double* total_ms, long long* launches, double* units,
+                    double* bytes) {
+  if (!h) return ABD_ERR_INVALID;
+  h->e.prof.flush();
+  int n = 0;
+  for (int t = 0; t < abd::K_NTAGS && n < max_n; ++t) {
+    if (names) {
+      std::strncpy(names + 32 * n, abd::kTagNames[t], 31);
+      names[32 * n + 31] = 0;
+    }
+    if (total_ms) total_ms[n] = h->e.prof.ms[t];
+    if (launches) launches[n] = h->e.prof.cnt[t];
+    if (units) units[n] = h->e.prof.units[t];
+    if (bytes) bytes[n] = h->e.prof.bytes[t];
+    ++n;
+  }
+  return n;
+}
 int abd_set_iter(abd_handle* h, int it) {
   if (!h) return ABD_ERR_INVALID;
   h->e.iter = it;

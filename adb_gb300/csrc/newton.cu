@@ -785,23 +785,23 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
   B.D.ensure(144 * (size_t)nb);
   B.Dinv.ensure(144 * (size_t)nb);
   B.grad.ensure(12 * (size_t)nb);
+  // pair terms: tuple 20 B + 4 world and 4 rest positions 192 B + lagged friction 200 B
+  prof_work(K_PAIR_TERMS, (double)npt + nee, 412.0 * ((double)npt + nee));
+  prof_work(K_OV_REDUCE, nov, 2.0 * 1152 * nov);
+  prof_work(K_BODY_SYSTEM, nb, 2.0 * 1152 * nb + 2 * 96.0 * nb);
   if (npt) {
-    k_pair_terms<<<nblk(npt, 128), 128, 0, s>>>(g, P, 0, npt, S.pt.p, S.pt_ov.p, S.ovI.p, B.pt_c.p, S.pt_lag.p);
-    CK(cudaGetLastError());
+    KLAUNCH(K_PAIR_TERMS, s, k_pair_terms<<<nblk(npt, 128), 128, 0, s>>>(g, P, 0, npt, S.pt.p, S.pt_ov.p, S.ovI.p, B.pt_c.p, S.pt_lag.p));
   }
   if (nee) {
-    k_pair_terms<<<nblk(nee, 128), 128, 0, s>>>(g, P, 1, nee, S.ee.p, S.ee_ov.p, S.ovI.p, B.ee_c.p, S.ee_lag.p);
-    CK(cudaGetLastError());
+    KLAUNCH(K_PAIR_TERMS, s, k_pair_terms<<<nblk(nee, 128), 128, 0, s>>>(g, P, 1, nee, S.ee.p, S.ee_ov.p, S.ovI.p, B.ee_c.p, S.ee_lag.p));
   }
   if (nov) {
-    k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, npt, S.pt_ov.p, B.pt_seg.p);
-    k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, nee, S.ee_ov.p, B.ee_seg.p);
-    k_ov_reduce<<<nov, 256, 0, s>>>(nov, B.pt_seg.p, B.ee_seg.p, B.pt_c.p, npt, B.ee_c.p, nee, B.ovr.p, B.has.p);
-    CK(cudaGetLastError());
+    KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, npt, S.pt_ov.p, B.pt_seg.p));
+    KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, nee, S.ee_ov.p, B.ee_seg.p));
+    KLAUNCH(K_OV_REDUCE, s, k_ov_reduce<<<nov, 256, 0, s>>>(nov, B.pt_seg.p, B.ee_seg.p, B.pt_c.p, npt, B.ee_c.p, nee, B.ovr.p, B.has.p));
   }
-  k_body_system<<<nb, 160, 0, s>>>(g, P, S.row_ptr.p, S.col.p, S.upidx.p, B.ovr.p, B.has.p, S.vg.p, S.vg_seg.p,
-                                   S.vg_lam.p, B.D.p, B.grad.p);
-  CK(cudaGetLastError());
+  KLAUNCH(K_BODY_SYSTEM, s, k_body_system<<<nb, 160, 0, s>>>(g, P, S.row_ptr.p, S.col.p, S.upidx.p, B.ovr.p, B.has.p, S.vg.p, S.vg_seg.p,
+                                   S.vg_lam.p, B.D.p, B.grad.p));
 }
 
 int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_iter, double* dq, cudaStream_t s,
@@ -810,8 +810,7 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   B.status.ensure(4);
   if (!B.h_int) CK(cudaMallocHost(&B.h_int, 16 * sizeof(int)));
   CK(cudaMemsetAsync(B.status.p, 0, 4 * sizeof(int), s));
-  k_block_inverse<<<nblk(nb, 64), 64, 0, s>>>(nb, B.D.p, B.Dinv.p, B.status.p);
-  CK(cudaGetLastError());
+  KLAUNCH(K_BLOCK_INVERSE, s, k_block_inverse<<<nblk(nb, 64), 64, 0, s>>>(nb, B.D.p, B.Dinv.p, B.status.p));
   B.x.ensure(12 * (size_t)nb);
   B.r.ensure(12 * (size_t)nb);
   B.z.ensure(12 * (size_t)nb);
@@ -850,10 +849,12 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   a.maxit = max_iter;
   a.out = B.status.p;
   void* args[] = {&a};
-  CK(cudaLaunchCooperativeKernel((void*)k_pcg, dim3(grid), dim3(256), args, 0, s));
+  KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel((void*)k_pcg, dim3(grid), dim3(256), args, 0, s)));
   CK(cudaMemcpyAsync(B.h_int, B.status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   *status = B.h_int[0];
+  // per iteration: the block matrix once (1152 B per block) and ~6 vector streams
+  prof_work(K_PCG, B.h_int[1], B.h_int[1] * (1152.0 * (nb + 2.0 * S.nov) + 6 * 96.0 * nb) + 1152.0 * nb);
   return B.h_int[1];
 }
 
@@ -882,10 +883,10 @@ double energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSe
   B.red.ensure(G + 8);
   a.partial = B.red.p;
   if (!B.h_red) CK(cudaMallocHost(&B.h_red, 16 * sizeof(double)));
-  k_energy<<<G, 256, 0, s>>>(g, P, a);
-  CK(cudaGetLastError());
-  k_final_sum<<<1, 256, 0, s>>>(B.red.p, G, B.red.p + G);
-  CK(cudaGetLastError());
+  prof_work(K_ENERGY, (double)a.npt + a.nee + a.lpt + a.lee,
+            136.0 * ((double)a.npt + a.nee + a.lpt + a.lee) + 96.0 * g.nb);
+  KLAUNCH(K_ENERGY, s, k_energy<<<G, 256, 0, s>>>(g, P, a));
+  KLAUNCH(K_ENERGY, s, k_final_sum<<<1, 256, 0, s>>>(B.red.p, G, B.red.p + G));
   CK(cudaMemcpyAsync(B.h_red, B.red.p + G, sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   return B.h_red[0];
@@ -895,9 +896,8 @@ void dots(int n, const double* dq, const double* grad, NewtonBufs& B, double* ou
   const int G = 64;
   B.red.ensure(3 * G + 8);
   if (!B.h_red) CK(cudaMallocHost(&B.h_red, 16 * sizeof(double)));
-  k_dots<<<G, 256, 0, s>>>(n, dq, grad, B.red.p);
-  k_dots_final<<<1, 32, 0, s>>>(B.red.p, G, B.red.p + 3 * G);
-  CK(cudaGetLastError());
+  KLAUNCH(K_DOTS, s, k_dots<<<G, 256, 0, s>>>(n, dq, grad, B.red.p));
+  KLAUNCH(K_DOTS, s, k_dots_final<<<1, 32, 0, s>>>(B.red.p, G, B.red.p + 3 * G));
   CK(cudaMemcpyAsync(B.h_red, B.red.p + 3 * G, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   out[0] = B.h_red[0];
@@ -907,23 +907,19 @@ void dots(int n, const double* dq, const double* grad, NewtonBufs& B, double* ou
 
 void launch_scale(double* v, int n, double sc, cudaStream_t st) {
   if (n <= 0) return;
-  k_scale<<<nblk(n, 256), 256, 0, st>>>(v, n, sc);
-  CK(cudaGetLastError());
+  KLAUNCH(K_VEC, st, k_scale<<<nblk(n, 256), 256, 0, st>>>(v, n, sc));
 }
 void launch_q_update(double* q, const double* dq, int n, double alpha, cudaStream_t st) {
   if (n <= 0) return;
-  k_q_update<<<nblk(n, 256), 256, 0, st>>>(q, dq, n, alpha);
-  CK(cudaGetLastError());
+  KLAUNCH(K_VEC, st, k_q_update<<<nblk(n, 256), 256, 0, st>>>(q, dq, n, alpha));
 }
 void launch_frame_end(double* q, double* q0, double* dqdt, int n, double dt, cudaStream_t st) {
   if (n <= 0) return;
-  k_frame_end<<<nblk(n, 256), 256, 0, st>>>(q, q0, dqdt, n, dt);
-  CK(cudaGetLastError());
+  KLAUNCH(K_VEC, st, k_frame_end<<<nblk(n, 256), 256, 0, st>>>(q, q0, dqdt, n, dt));
 }
 void launch_copy(double* d, const double* s_, int n, cudaStream_t st) {
   if (n <= 0) return;
-  k_copy<<<nblk(n, 256), 256, 0, st>>>(d, s_, n);
-  CK(cudaGetLastError());
+  KLAUNCH(K_VEC, st, k_copy<<<nblk(n, 256), 256, 0, st>>>(d, s_, n));
 }
 
 }  // namespace abd

@@ -84,12 +84,10 @@ void scan_rec(const T* in, T* out, int n, cudaStream_t s, T* tmp, size_t tmp_cap
   T* sums = tmp;
   T* sums_off = tmp + tiles;
   if ((size_t)(2 * tiles) > tmp_cap) throw CudaError{cudaErrorMemoryAllocation, "scan scratch"};
-  k_scan_tiles<T><<<tiles, SCAN_T, 0, s>>>(in, out, n, sums);
-  CK(cudaGetLastError());
+  KLAUNCH(K_SCAN, s, (k_scan_tiles<T><<<tiles, SCAN_T, 0, s>>>(in, out, n, sums)));
   if (tiles > 1) {
     scan_rec<T>(sums, sums_off, tiles, s, tmp + 2 * tiles, tmp_cap - 2 * tiles);
-    k_scan_add<T><<<tiles, SCAN_T, 0, s>>>(out, n, sums_off);
-    CK(cudaGetLastError());
+    KLAUNCH(K_SCAN, s, (k_scan_add<T><<<tiles, SCAN_T, 0, s>>>(out, n, sums_off)));
   }
 }
 
@@ -109,9 +107,8 @@ void scan_exclusive_int(const int* in, int* out, int n, int* d_total, cudaStream
   tmp.ensure(scan_scratch<int>(n) + 8);
   scan_rec<int>(in, out, n, s, tmp.p, tmp.cap);
   if (d_total) {
-    if (n > 0) k_total<int><<<1, 32, 0, s>>>(in, out, n, d_total);
+    if (n > 0) KLAUNCH(K_SCAN, s, (k_total<int><<<1, 32, 0, s>>>(in, out, n, d_total)));
     else CK(cudaMemsetAsync(d_total, 0, sizeof(int), s));
-    CK(cudaGetLastError());
   }
 }
 
@@ -120,9 +117,8 @@ void scan_exclusive_ll(const long long* in, long long* out, int n, long long* d_
   tmp.ensure(scan_scratch<long long>(n) + 8);
   scan_rec<long long>(in, out, n, s, tmp.p, tmp.cap);
   if (d_total) {
-    if (n > 0) k_total<long long><<<1, 32, 0, s>>>(in, out, n, d_total);
+    if (n > 0) KLAUNCH(K_SCAN, s, (k_total<long long><<<1, 32, 0, s>>>(in, out, n, d_total)));
     else CK(cudaMemsetAsync(d_total, 0, sizeof(long long), s));
-    CK(cudaGetLastError());
   }
 }
 

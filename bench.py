@@ -1,0 +1,306 @@
+"""Benchmark of the GB300 affine-body contact step.
+
+Workload: the 1024-body icosphere pile (16 x 16 x 4 grid of subdivision-3 icospheres,
+radius 0.5, spacing 1.1, seeded rotation / jitter / velocity; dt 0.01, dhat 1e-3,
+mu 0.1, Newton tol 1e-4), started from its committed contact-rich checkpoint
+(adb_gb300/data/pile_ckpt.npz, written by adb_gb300/data/make_checkpoint.py) so that
+every timed frame carries the full contact load. A step is one frame
+(ABD::implicit_euler). Metric: frames/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+gb300 arm: W untimed frames, then K frames timed with CUDA events on the engine's
+stream (value, state resident in HBM), then the same K frames again through the public
+C ABI with host buffers (e2e: pinned host state -> device, step, device -> host every
+frame), then one profiled pass for the per-kernel roofline. N > 1 runs N independent
+replicas (one per GPU; the pile does not shard): value = total frames/s of all ranks
+over the max-over-ranks time.
+reference arm: the CPU restatement of the reference (oracle/, OpenMP on all host
+cores) on the same checkpoint, each step one frame, bounded by a time budget.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s, 1024-body pile GPU vs CPU ref; batched vs looped scenes/s at tol"
+CKPT = os.path.join(ROOT, "adb_gb300", "data", "pile_ckpt.npz")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.md")
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def pile_workload():
+    from adb_gb300 import scene as S
+    sc = S.sphere_pile(seed=0)
+    cfg = S.workload_config("pile")
+    q0, qd, frame = sc.q0, sc.dqdt, 0
+    if os.path.exists(CKPT):
+        z = np.load(CKPT)
+        q0, qd, frame = z["q0"], z["qdot"], int(z["frame"])
+    return sc, cfg, q0, qd, frame
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_unit(kernel):
+    """DRAM bytes per work unit of `kernel` from the committed ncu summary, if any."""
+    if not os.path.exists(PROFILE_TRAFFIC):
+        return None
+    for line in open(PROFILE_TRAFFIC):
+        if line.startswith("traffic_per_unit") and kernel in line:
+            try:
+                return float(line.split("=")[1].split()[0])
+            except Exception:
+                return None
+    return None
+
+
+def cpu_baseline_frames(sc, cfg, q0, qd, frames_budget_s=90.0, max_frames=3):
+    """The CPU restatement on all host cores, one frame at a time from the checkpoint."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    sim = O.OracleSim(sc, cfg, n_threads=cores)
+    sim.set_state(q0, qd)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_frames:
+        st = sim.step(1)
+        n += 1
+        if st.status != 0 or time.perf_counter() - t0 > frames_budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return n / dt, cores, n, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sc, cfg, q0, qd, frame = pile_workload()
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    sim = O.OracleSim(sc, cfg, n_threads=cores)
+    sim.set_state(q0, qd)
+    budget = float(os.environ.get("ABD_REF_BUDGET_S", "150"))
+    t0 = time.perf_counter()
+    n = 0
+    # each step is one frame; the run stops at the time budget (at least one frame)
+    for _ in range(max(1, args.steps)):
+        st = sim.step(1)
+        n += 1
+        if st.status != 0 or time.perf_counter() - t0 > budget:
+            break
+    dt = time.perf_counter() - t0
+    v = n / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": n, "warmup": 0, "ms_per_step": 1000.0 * dt / n, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "pile-1024 icosphere-s3 from frame-%d checkpoint" % frame, "bodies": sc.n_bodies,
+                       "vertices": sc.n_vertices, "dt": cfg.dt, "dhat": cfg.dhat, "mu": cfg.mu, "tol": cfg.tol},
+            "cpu_baseline": {"value": v, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": "%d frame(s) of the pile from the checkpoint, all host cores" % n},
+            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    rank, world, local = dist_env()
+    import ctypes as C
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import __graft_entry__ as G
+    G.build()
+    from adb_gb300 import _lib as L
+    from adb_gb300.abd import ABD, measure_fp64_gflops
+
+    sc, cfg, q0, qd, frame = pile_workload()
+    sim = ABD(sc, cfg)
+
+    def barrier():
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    # ---- value: W untimed frames, then K frames with the state resident on the device ----
+    sim.set_state(q0, qd)
+    if args.warmup:
+        sim.step(args.warmup)
+    start_q, start_qd = sim.state()
+    barrier()
+    with ClockSampler(local) as clk:
+        st = sim.step(args.steps)
+    barrier()
+    dev_s = st.device_ms / 1000.0
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = world * args.steps / dev_s
+    clocks = clk.summary()
+
+    # ---- e2e: same frames through the public API with host buffers ----
+    lib = L.lib()
+    hq = np.ascontiguousarray(start_q)
+    hqd = np.ascontiguousarray(start_qd)
+    outq = np.zeros_like(hq)
+    outqd = np.zeros_like(hqd)
+    h2d = hq.nbytes + hqd.nbytes
+    d2h = outq.nbytes + outqd.nbytes
+    barrier()
+    t0 = time.perf_counter()
+    est = L.AbdFrameStats()
+    for k in range(args.steps):
+        lib.abd_set_state(sim._h, L.dptr(hq), L.dptr(hqd))
+        lib.abd_step(sim._h, 0.0, 1, C.byref(est))
+        lib.abd_get_state(sim._h, L.dptr(outq), L.dptr(outqd))
+        hq, hqd = outq.copy(), outqd.copy()
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * args.steps / e2e_s
+
+    # ---- per-kernel device time (separate profiled pass over the same frames) ----
+    sim.set_state(start_q, start_qd)
+    sim.profile(True)
+    pst = sim.step(args.steps)
+    kt = sim.kernel_times()
+    sim.profile(False)
+    tot = sum(v["ms"] for v in kt.values())
+    dom = max(kt, key=lambda k: kt[k]["ms"])
+    d = kt[dom]
+    peak, peak_kind = measured_peaks()
+    avg_ms = d["ms"] / max(d["launches"], 1)
+    bytes_per_launch = d["bytes"] / max(d["launches"], 1)
+    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    tpu = ncu_traffic_per_unit(dom)
+    traffic = tpu * d["units"] / max(d["launches"], 1) if tpu else None
+    fp64_peak = measure_fp64_gflops()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded icosphere pile, no dataset)",
+            "config": {"workload": "pile-1024 icosphere-s3 from frame-%d checkpoint" % frame,
+                       "bodies": sc.n_bodies, "vertices": sc.n_vertices, "dt": cfg.dt, "dhat": cfg.dhat,
+                       "mu": cfg.mu, "tol": cfg.tol, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "per-frame working set (positions, primitive boxes, pair records) >> 129 MB L2"},
+            "clocks": clocks,
+            "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(st.kernel_launches),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                         "traffic": traffic, "avg_launch_ms": avg_ms, "launches": d["launches"],
+                         "share": d["ms"] / tot if tot else None},
+            "fp64": {"peak_gflops_measured": fp64_peak},
+            "frame_stats": {"newton_iters": st.newton_iters, "ls_trials": st.ls_trials, "pcg_iters": st.pcg_iters,
+                            "max_pt": st.n_pt, "max_ee": st.n_ee, "max_vg": st.n_vg,
+                            "algorithmic_GB": st.bytes_moved / 1e9},
+            "kernel_ms": {k: round(v["ms"], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1]["ms"])
+                          if v["ms"] > 0},
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            v, cores, n, secs = cpu_baseline_frames(sc, cfg, start_q, start_qd, frames_budget_s=60.0, max_frames=1)
+            line["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": cores, "kind": "port",
+                                    "sample": "%d frame of the pile from the same state (%.1f s)" % (n, secs)}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -81,9 +81,11 @@ typedef struct {
   int n_pt, n_ee, n_vg, n_overlaps; /* maxima over the frames */
   int status;
   int pad;
+  long long kernel_launches;                        /* kernels launched by these frames */
   double toi_min, alpha_min;
   double t_ipc_ms, t_solver_ms, t_ccd_ms, t_ls_ms; /* reference's 4-phase breakdown */
   double bytes_moved;                               /* algorithmic bytes of the path */
+  double device_ms;                                 /* CUDA-event time of the call on the handle's stream */
 } abd_frame_stats;
 
 typedef struct abd_handle abd_handle;
@@ -103,6 +105,16 @@ int abd_get_iter(abd_handle* h);
 int abd_set_iter(abd_handle* h, int iter);
 const char* abd_last_error(abd_handle* h);
 void abd_destroy(abd_handle* h);
+/* Per-kernel device timing: when enabled, every kernel of the step is bracketed with
+ * CUDA events on the handle's stream. abd_kernel_times returns the number of kernel
+ * classes (<= max_n), their names (32 chars each), total ms and launch counts since the
+ * last abd_profile call. */
+int abd_profile(abd_handle* h, int enable);
+int abd_kernel_times(abd_handle* h, int max_n, char* names, double* total_ms, long long* launches);
+/* As abd_kernel_times, plus each class's work units (pairs, candidates, rows, ...) and
+ * algorithmic bytes (per-unit figure x units) over the same launches. */
+int abd_kernel_work(abd_handle* h, int max_n, char* names, double* total_ms, long long* launches, double* units,
+                    double* bytes);
 
 /* ---- stage entry points (parity tests and profiling) ---- */
 /* Culls at state q (+ dq): vtn 1 at q, 2 at q + dq, 3 the trajectory q -> q + dq.

@@ -1,0 +1,202 @@
+"""GPU path (libabd_gb300.so, called through the C ABI) against the CPU oracle.
+
+Bar: pair sets and distance types bit-exact; TOIs bit-exact; per-pair energy, gradient
+and Hessian within 1e-9 relative; Newton systems within 1e-9 relative; per-frame
+states within 1e-9 relative (relative to the largest state entry)."""
+import numpy as np
+import pytest
+
+from adb_gb300 import abdtk
+from adb_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-9
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def O(gpu_lib, oracle_lib):
+    return oracle_lib
+
+
+def ABD(scene, cfg):
+    from adb_gb300.abd import ABD as _ABD
+    return _ABD(scene, cfg)
+
+
+def rand_cubes(n, seed, extent):
+    rng = np.random.default_rng(seed)
+    sb = S.SceneBuilder()
+    for _ in range(n):
+        a, b, c = rng.random(3) * 2 * np.pi
+        sb.add(S.cube_mesh(), rng.uniform(-extent, extent, 3), S.rotation_zyx(a, b, c))
+    return sb.build()
+
+
+def assert_sets_equal(g, o):
+    for name, a, b in zip(("pt", "pt_type", "ee", "ee_type", "vg"), g, o):
+        assert a.shape == b.shape and np.array_equal(a, b), name
+
+
+def test_cull_bit_exact_random_cubes(O):
+    sc = rand_cubes(30, 1, 1.8)
+    cfg = S.Config(dhat=1e-2)
+    gpu, orc = ABD(sc, cfg), O.OracleSim(sc, cfg)
+    g, o = gpu.cull(1, sc.q0), orc.cull(1, sc.q0)
+    assert len(o[0]) + len(o[2]) > 50
+    assert_sets_equal(g, o)
+    rng = np.random.default_rng(2)
+    dq = rng.normal(size=sc.q0.shape) * 0.02
+    assert_sets_equal(gpu.cull(2, sc.q0, dq), orc.cull(2, sc.q0, dq))
+    assert gpu.cull(3, sc.q0, dq) == orc.cull(3, sc.q0, dq)
+
+
+def test_cull_bit_exact_along_cube_stack_run(O):
+    sc = S.cube_stack(10, seed=0)
+    cfg = S.workload_config("cubes")
+    gpu, orc = ABD(sc, cfg), O.OracleSim(sc, cfg)
+    rng = np.random.default_rng(3)
+    n_checked = 0
+    for f in range(48):
+        orc.step(1)
+        if f % 6 == 5:
+            q0, _ = orc.state()
+            g, o = gpu.cull(1, q0), orc.cull(1, q0)
+            assert_sets_equal(g, o)
+            n_checked += len(o[2]) + len(o[4])
+            dq = rng.normal(size=q0.shape) * 1e-2
+            assert gpu.cull(3, q0, dq) == orc.cull(3, q0, dq)
+    assert n_checked > 0
+
+
+def test_cull_bit_exact_sphere_pile(O):
+    sc = S.sphere_pile(4, 4, 2, subdiv=2, seed=1)
+    cfg = S.workload_config("pile")
+    orc = O.OracleSim(sc, cfg)
+    orc.step(25)
+    q0, _ = orc.state()
+    gpu = ABD(sc, cfg)
+    g, o = gpu.cull(1, q0), orc.cull(1, q0)
+    assert len(o[0]) > 0 and len(o[2]) > 0
+    assert_sets_equal(g, o)
+
+
+def test_distance_types_and_tois_bit_exact(O):
+    rng = np.random.default_rng(4)
+    X = rng.normal(size=(3000, 4, 3)) * 0.02
+    t, d = abdtk.pt_distance_batch(X)
+    assert np.array_equal(t, [O.pt_type(x.ravel()) for x in X])
+    assert np.array_equal(d, [O.pt_dist(x.ravel(), k) for x, k in zip(X, t)])
+    t, d = abdtk.ee_distance_batch(X)
+    assert np.array_equal(t, [O.ee_type(x.ravel()) for x in X])
+    assert np.array_equal(d, [O.ee_dist(x.ravel(), k) for x, k in zip(X, t)])
+    Y = rng.random((3000, 8, 3))
+    assert np.array_equal(abdtk.pt_collision_time_batch(Y), [O.pt_collision_time(y.ravel()) for y in Y])
+    assert np.array_equal(abdtk.ee_collision_time_batch(Y), [O.ee_collision_time(y.ravel()) for y in Y])
+
+
+def test_known_answer_toi_on_gpu():
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "pt_toi_known.npz"))
+    x = np.concatenate([z["p0"][:, None], z["tri"], z["p1"][:, None], z["tri"]], axis=1)
+    toi = abdtk.pt_collision_time_batch(x)
+    assert np.abs(toi - z["toi"]).max() < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["pt", "ee"])
+def test_pair_hessians_match_oracle(O, kind):
+    rng = np.random.default_rng(5)
+    X = rng.normal(size=(400, 4, 3)) * 0.02
+    if kind == "pt":
+        t, d = abdtk.pt_distance_batch(X)
+    else:
+        t, d = abdtk.ee_distance_batch(X)
+        X[:50, 3] = X[:50, 2] + (X[:50, 1] - X[:50, 0]) * 1.3 + 1e-4 * rng.normal(size=(50, 3))
+        t, d = abdtk.ee_distance_batch(X)
+    dhat = float(d.max()) * 2
+    abdtk.set_params(dhat=dhat, kappa=0.5, eps_x=1e-3, psd=True)
+    try:
+        if kind == "pt":
+            H, g = abdtk.ipc_hess_pt_batch(X, t, d)
+        else:
+            H, g, m = abdtk.ipc_hess_ee_batch(X, t, d)
+    finally:
+        abdtk.set_params(dhat=1e-4, kappa=1e-3)
+    for i in range(len(X)):
+        if kind == "pt":
+            Ho, go = O.ipc_hess_pt(X[i].ravel(), t[i], d[i], dhat, 0.5)
+        else:
+            Ho, go, mo = O.ipc_hess_ee(X[i].ravel(), t[i], d[i], dhat, 0.5, 1e-3)
+            assert abs(m[i] - mo) <= 1e-12
+        assert rel(H[i], Ho) <= REL and rel(g[i], go) <= REL
+
+
+def test_newton_system_matches_oracle(O):
+    sc = S.cube_stack(6, seed=2)
+    cfg = S.workload_config("cubes")
+    orc = O.OracleSim(sc, cfg)
+    orc.step(30)
+    q0, qd = orc.state()
+    gpu = ABD(sc, cfg)
+    gpu.set_state(q0, qd)
+    rng = np.random.default_rng(6)
+    q = q0 + rng.normal(size=q0.shape) * 1e-4
+    gg, gd, gk, gv = gpu.newton_system(q)
+    og, od, ok, ov = orc_system(O, sc, cfg, q0, qd, q)
+    assert np.array_equal(gk, ok)
+    assert rel(gg, og) <= REL and rel(gd, od) <= REL
+    if len(ov):
+        assert rel(gv, ov) <= REL
+    gdq, its = gpu.newton_dq(q)
+    assert rel(gdq, orc_dq(O, sc, cfg, q0, qd, q)) <= 1e-7
+
+
+def orc_system(O, sc, cfg, q0, qd, q):
+    o = O.OracleSim(sc, cfg)
+    o.set_state(q0, qd)
+    return o.newton_system(q)
+
+
+def orc_dq(O, sc, cfg, q0, qd, q):
+    o = O.OracleSim(sc, cfg)
+    o.set_state(q0, qd)
+    return o.newton_dq(q)
+
+
+def run_pair(O, sc, cfg, frames):
+    """Steps both implementations frame by frame; before every frame the GPU state is
+    reset to the oracle's, so each comparison is one frame from the same start state."""
+    gpu, orc = ABD(sc, cfg), O.OracleSim(sc, cfg)
+    worst = 0.0
+    for _ in range(frames):
+        q0, qd = orc.state()
+        gpu.set_state(q0, qd)
+        gpu.iter = orc.iter
+        sg = gpu.implicit_euler()
+        so = orc.step(1)
+        assert sg.status in (0, 6) and so.status == 0
+        qg, vg = gpu.state()
+        qo, vo = orc.state()
+        worst = max(worst, rel(qg, qo))
+        assert gpu.iter == orc.iter
+    return worst
+
+
+def test_frames_match_oracle_cube_stack(O):
+    worst = run_pair(O, S.cube_stack(10, seed=0), S.workload_config("cubes"), 60)
+    assert worst <= REL
+
+
+def test_frames_match_oracle_small_pile(O):
+    worst = run_pair(O, S.sphere_pile(3, 3, 2, subdiv=1, seed=2), S.workload_config("pile"), 30)
+    assert worst <= REL
+
+
+def test_frames_match_oracle_chain_with_static_link(O):
+    cfg = S.workload_config("chain")
+    worst = run_pair(O, S.torus_chain(4, nu=16, nv=8, seed=3), cfg, 20)
+    assert worst <= REL
