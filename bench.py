@@ -173,10 +173,11 @@ def run_gb300(args):
     import ctypes as C
 
     if world > 1:
-        import torch
+        # one replica per GPU: this rank's library sees only its own device
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        os.environ["CUDA_VISIBLE_DEVICES"] = vis.split(",")[local] if vis else str(local)
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        dist.init_process_group("gloo")
     import __graft_entry__ as G
     G.build()
     from adb_gb300 import _lib as L
@@ -186,11 +187,19 @@ def run_gb300(args):
     sim = ABD(sc, cfg)
 
     def barrier():
+        # abd_step returns after synchronising its stream, so a host barrier suffices
         if world > 1:
-            import torch
             import torch.distributed as dist
             dist.barrier()
-            torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
 
     # ---- value: W untimed frames, then K frames with the state resident on the device ----
     sim.set_state(q0, qd)
@@ -198,16 +207,10 @@ def run_gb300(args):
         sim.step(args.warmup)
     start_q, start_qd = sim.state()
     barrier()
-    with ClockSampler(local) as clk:
+    with ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if world > 1 else 0) as clk:
         st = sim.step(args.steps)
     barrier()
-    dev_s = st.device_ms / 1000.0
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s = float(t.item())
+    dev_s = max_over_ranks(st.device_ms / 1000.0)
     value = world * args.steps / dev_s
     clocks = clk.summary()
 
@@ -227,14 +230,8 @@ def run_gb300(args):
         lib.abd_step(sim._h, 0.0, 1, C.byref(est))
         lib.abd_get_state(sim._h, L.dptr(outq), L.dptr(outqd))
         hq, hqd = outq.copy(), outqd.copy()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
     barrier()
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
     e2e = world * args.steps / e2e_s
 
     # ---- per-kernel device time (separate profiled pass over the same frames) ----
