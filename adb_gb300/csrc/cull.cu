@@ -249,174 +249,12 @@ __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const 
   }
 }
 
-__global__ void k_cand_count(int nov, const int* cnt, long long* cc) {
-  int u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= nov) return;
-  const int* c = cnt + 6 * u;
-  cc[u] = (long long)c[0] * c[5] + (long long)c[3] * c[2] + (long long)c[1] * c[4];
-}
-
-struct Cand {
-  int sub;       // 0: v(I) x f(J), 1: v(J) x f(I), 2: e(I) x e(J)
-  int A, B;      // bodies of the first / second primitive
-  int a, b;      // local primitive ids
-};
-
-__device__ __forceinline__ Cand decode(long long c, int nov, const long long* cand_off, const int* cnt, const int* off,
-                                       const int* lst, const int* ovI, const int* ovJ, int& u_out) {
-  int lo = 0, hi = nov;  // largest u with cand_off[u] <= c
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (cand_off[mid] <= c) lo = mid;
-    else hi = mid;
-  }
-  int u = lo;
-  u_out = u;
-  long long l = c - cand_off[u];
-  const int* n = cnt + 6 * u;
-  const int* o = off + 6 * u;
-  long long s0 = (long long)n[0] * n[5], s1 = (long long)n[3] * n[2];
-  Cand r;
-  int I = ovI[u], J = ovJ[u];
-  if (l < s0) {
-    r.sub = 0;
-    int i = (int)(l / n[5]), j = (int)(l % n[5]);
-    r.A = I; r.a = lst[o[0] + i]; r.B = J; r.b = lst[o[5] + j];
-  } else if (l < s0 + s1) {
-    l -= s0;
-    r.sub = 1;
-    int i = (int)(l / n[2]), j = (int)(l % n[2]);
-    r.A = J; r.a = lst[o[3] + i]; r.B = I; r.b = lst[o[2] + j];
-  } else {
-    l -= s0 + s1;
-    r.sub = 2;
-    int i = (int)(l / n[4]), j = (int)(l % n[4]);
-    r.A = I; r.a = lst[o[1] + i]; r.B = J; r.b = lst[o[4] + j];
-  }
-  return r;
-}
-
-constexpr int NT = 256;   // narrow-phase threads per CTA
-constexpr int NI = 8;     // candidates per thread
-constexpr int NTILE = NT * NI;
+constexpr int NT = 256;     // narrow-phase threads per CTA
+constexpr int TILE = 1000;  // primitives of one list staged in shared memory (2 x 24 kB)
 
 __device__ __forceinline__ void finflate(const float* s, float ds, float* o) {
   o[0] = __fsub_rd(s[0], ds); o[1] = __fsub_rd(s[1], ds); o[2] = __fsub_rd(s[2], ds);
   o[3] = __fadd_ru(s[3], ds); o[4] = __fadd_ru(s[4], ds); o[5] = __fadd_ru(s[5], ds);
-}
-
-// Classifies one candidate. Returns 0 (no pair), 1 + type (PT) or 16 + type (EE).
-__device__ __forceinline__ int classify(const Geo& g, const Params& P, float ds_f, const Cand& cd, const float* vb,
-                                        const float* eb, const float* fb) {
-  int nv = g.nv;
-  if (cd.sub < 2) {
-    int v = g.v_off[cd.A] + cd.a, f = g.f_off[cd.B] + cd.b;
-    float vi[6];
-    finflate(vb + 6 * v, ds_f, vi);
-    if (!f_overlap(vi, fb + 6 * f)) return 0;
-    d3 p = ldX(g.X, nv, v);
-    box bv = inflate(box{p, p}, P.d_sqrt);
-    d3 t0 = ldX(g.X, nv, g.fv[3 * f]), t1 = ldX(g.X, nv, g.fv[3 * f + 1]), t2 = ldX(g.X, nv, g.fv[3 * f + 2]);
-    if (!overlaps(bv, box3(t0, t1, t2))) return 0;
-    int ty = pt_type(p, t0, t1, t2);
-    double d = pt_dist(p, t0, t1, t2, ty);
-    return (d < P.dhat) ? 1 + ty : 0;
-  } else {
-    int ea = g.e_off[cd.A] + cd.a, ebi = g.e_off[cd.B] + cd.b;
-    float ei[6];
-    finflate(eb + 6 * ea, ds_f, ei);
-    if (!f_overlap(ei, eb + 6 * ebi)) return 0;
-    d3 a0 = ldX(g.X, nv, g.ev[2 * ea]), a1 = ldX(g.X, nv, g.ev[2 * ea + 1]);
-    d3 b0 = ldX(g.X, nv, g.ev[2 * ebi]), b1 = ldX(g.X, nv, g.ev[2 * ebi + 1]);
-    if (!overlaps(inflate(box2(a0, a1), P.d_sqrt), box2(b0, b1))) return 0;
-    int ty = ee_type(a0, a1, b0, b1);
-    double d = ee_dist(a0, a1, b0, b1, ty);
-    return (d < P.dhat) ? 16 + ty : 0;
-  }
-}
-
-// 5a. narrow phase, pass 0: flags + per-CTA counts of PT and EE pairs
-__global__ void __launch_bounds__(NT) k_narrow_flags(Geo g, Params P, float ds_f, int nov, long long total,
-                                                     const long long* cand_off, const int* cnt, const int* off,
-                                                     const int* lst, const int* ovI, const int* ovJ, const float* vb,
-                                                     const float* eb, const float* fb, uint8_t* flags, int* blk_pt,
-                                                     int* blk_ee) {
-  __shared__ int sp[NT / 32], se[NT / 32];
-  long long base = (long long)blockIdx.x * NTILE;
-  int cpt = 0, cee = 0;
-#pragma unroll 1
-  for (int k = 0; k < NI; ++k) {
-    long long c = base + (long long)k * NT + threadIdx.x;
-    int f = 0;
-    if (c < total) {
-      int u;
-      Cand cd = decode(c, nov, cand_off, cnt, off, lst, ovI, ovJ, u);
-      f = classify(g, P, ds_f, cd, vb, eb, fb);
-      flags[c] = (uint8_t)f;
-    }
-    cpt += (f >= 1 && f < 16);
-    cee += (f >= 16);
-  }
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    cpt += __shfl_xor_sync(0xffffffffu, cpt, o);
-    cee += __shfl_xor_sync(0xffffffffu, cee, o);
-  }
-  if (lane == 0) { sp[w] = cpt; se[w] = cee; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int a = 0, b = 0;
-    for (int i = 0; i < NT / 32; ++i) { a += sp[i]; b += se[i]; }
-    blk_pt[blockIdx.x] = a;
-    blk_ee[blockIdx.x] = b;
-  }
-}
-
-// 5b. narrow phase, pass 1: ordered compaction of the flagged candidates
-__global__ void __launch_bounds__(NT) k_narrow_write(int nov, long long total, const long long* cand_off,
-                                                     const int* cnt, const int* off, const int* lst, const int* ovI,
-                                                     const int* ovJ, const uint8_t* flags, const int* blk_pt_off,
-                                                     const int* blk_ee_off, int* pt, int8_t* pt_ty, int* pt_ov,
-                                                     int* ee, int8_t* ee_ty, int* ee_ov) {
-  __shared__ int wp[NT / 32], we[NT / 32];
-  long long base = (long long)blockIdx.x * NTILE;
-  int run_pt = blk_pt_off[blockIdx.x], run_ee = blk_ee_off[blockIdx.x];
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  unsigned below = (1u << lane) - 1u;
-#pragma unroll 1
-  for (int k = 0; k < NI; ++k) {
-    long long c = base + (long long)k * NT + threadIdx.x;
-    int f = (c < total) ? flags[c] : 0;
-    bool ip = f >= 1 && f < 16, ie = f >= 16;
-    unsigned mp = __ballot_sync(0xffffffffu, ip), me = __ballot_sync(0xffffffffu, ie);
-    if (lane == 0) { wp[w] = __popc(mp); we[w] = __popc(me); }
-    __syncthreads();
-    int pre_p = 0, pre_e = 0, tot_p = 0, tot_e = 0;
-    for (int i = 0; i < NT / 32; ++i) {
-      if (i < w) { pre_p += wp[i]; pre_e += we[i]; }
-      tot_p += wp[i];
-      tot_e += we[i];
-    }
-    if (ip || ie) {
-      int u;
-      Cand cd = decode(c, nov, cand_off, cnt, off, lst, ovI, ovJ, u);
-      if (ip) {
-        int idx = run_pt + pre_p + __popc(mp & below);
-        pt[4 * idx] = cd.A; pt[4 * idx + 1] = cd.a; pt[4 * idx + 2] = cd.B; pt[4 * idx + 3] = cd.b;
-        pt_ty[idx] = (int8_t)(f - 1);
-        pt_ov[idx] = u;
-      } else {
-        int idx = run_ee + pre_e + __popc(me & below);
-        ee[4 * idx] = cd.A; ee[4 * idx + 1] = cd.a; ee[4 * idx + 2] = cd.B; ee[4 * idx + 3] = cd.b;
-        ee_ty[idx] = (int8_t)(f - 16);
-        ee_ov[idx] = u;
-      }
-    }
-    run_pt += tot_p;
-    run_ee += tot_e;
-    __syncthreads();
-  }
 }
 
 // Order-preserving key of a double for atomicMin on unsigned 64-bit.
@@ -425,42 +263,188 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
-// 5c. trajectory narrow phase: time of impact (atomic min over candidates)
-__global__ void __launch_bounds__(NT) k_narrow_toi(Geo g, int nov, long long total, const long long* cand_off,
-                                                   const int* cnt, const int* off, const int* lst, const int* ovI,
-                                                   const int* ovJ, const float* vb, const float* eb, const float* fb,
-                                                   unsigned long long* toi_key) {
-  long long base = (long long)blockIdx.x * NTILE;
-  double tmin = 1.0;
+// Exact narrow-phase test of one candidate at the culled configuration (vtn 1/2):
+// returns 0 (no pair) or 1 + distance type. sub 0/1: vertex v (global) of body A vs
+// face f (global) of body B; sub 2: edge ea vs edge eb.
+__device__ __forceinline__ int exact_pair(const Geo& g, const Params& P, int sub, int pa, int pb) {
   int nv = g.nv;
+  if (sub < 2) {
+    d3 p = ldX(g.X, nv, pa);
+    box bv = inflate(box{p, p}, P.d_sqrt);
+    d3 t0 = ldX(g.X, nv, g.fv[3 * pb]), t1 = ldX(g.X, nv, g.fv[3 * pb + 1]), t2 = ldX(g.X, nv, g.fv[3 * pb + 2]);
+    if (!overlaps(bv, box3(t0, t1, t2))) return 0;
+    int ty = pt_type(p, t0, t1, t2);
+    return (pt_dist(p, t0, t1, t2, ty) < P.dhat) ? 1 + ty : 0;
+  }
+  d3 a0 = ldX(g.X, nv, g.ev[2 * pa]), a1 = ldX(g.X, nv, g.ev[2 * pa + 1]);
+  d3 b0 = ldX(g.X, nv, g.ev[2 * pb]), b1 = ldX(g.X, nv, g.ev[2 * pb + 1]);
+  if (!overlaps(inflate(box2(a0, a1), P.d_sqrt), box2(b0, b1))) return 0;
+  int ty = ee_type(a0, a1, b0, b1);
+  return (ee_dist(a0, a1, b0, b1, ty) < P.dhat) ? 1 + ty : 0;
+}
+
+// Trajectory time of impact of one candidate (vtn 3), exact box test included.
+__device__ __forceinline__ double exact_toi(const Geo& g, int sub, int pa, int pb) {
+  int nv = g.nv;
+  if (sub < 2) {
+    d3 v1 = ldX(g.X, nv, pa), v0 = ldX(g.Xq, nv, pa);
+    int i0 = g.fv[3 * pb], i1 = g.fv[3 * pb + 1], i2 = g.fv[3 * pb + 2];
+    d3 f1[3] = {ldX(g.X, nv, i0), ldX(g.X, nv, i1), ldX(g.X, nv, i2)};
+    d3 f0[3] = {ldX(g.Xq, nv, i0), ldX(g.Xq, nv, i1), ldX(g.Xq, nv, i2)};
+    if (!overlaps(box2(v0, v1), merge(box3(f0[0], f0[1], f0[2]), box3(f1[0], f1[1], f1[2])))) return 1.0;
+    return pt_collision_time(v0, f0, v1, f1);
+  }
+  int a0 = g.ev[2 * pa], a1 = g.ev[2 * pa + 1], b0 = g.ev[2 * pb], b1 = g.ev[2 * pb + 1];
+  d3 A1[2] = {ldX(g.X, nv, a0), ldX(g.X, nv, a1)}, A0[2] = {ldX(g.Xq, nv, a0), ldX(g.Xq, nv, a1)};
+  d3 B1[2] = {ldX(g.X, nv, b0), ldX(g.X, nv, b1)}, B0[2] = {ldX(g.Xq, nv, b0), ldX(g.Xq, nv, b1)};
+  if (!overlaps(box4(A0[0], A0[1], A1[0], A1[1]), box4(B0[0], B0[1], B1[0], B1[1]))) return 1.0;
+  return ee_collision_time(A0, B0, A1, B1);
+}
+
+struct NarrowOut {
+  int *pt, *pt_ov, *ee, *ee_ov;
+  int8_t *pt_ty, *ee_ty;
+};
+
+// 5. Narrow phase, one CTA per overlap. For each of the three sub-problems
+// (v(I) x f(J), v(J) x f(I), e(I) x e(J)) the float boxes of both lists are staged in
+// shared memory (chunks of TILE), every (i, j) is tested in row-major order with the
+// outward-rounded float boxes, and the survivors get the exact test.
+// MODE 0: per-overlap PT/EE counts; MODE 1: ordered write at the scanned offsets;
+// MODE 2: trajectory TOI (atomic min).
+template <int MODE>
+__global__ void __launch_bounds__(NT) k_narrow_ov(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
+                                                  const int* cnt, const int* off, const int* lst, const float* vb,
+                                                  const float* eb, const float* fb, int* ov_npt, int* ov_nee,
+                                                  const int* ov_pt_off, const int* ov_ee_off, NarrowOut out,
+                                                  unsigned long long* toi_key) {
+  __shared__ float sA[TILE * 6], sB[TILE * 6];
+  __shared__ int wcnt[NT / 32];
+  const int u = blockIdx.x;
+  const int I = ovI[u], J = ovJ[u];
+  const int* n = cnt + 6 * u;
+  const int* o = off + 6 * u;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  int run_pt = (MODE == 1) ? ov_pt_off[u] : 0, run_ee = (MODE == 1) ? ov_ee_off[u] : 0;
+  double tmin = 1.0;
 #pragma unroll 1
-  for (int k = 0; k < NI; ++k) {
-    long long c = base + (long long)k * NT + threadIdx.x;
-    if (c >= total) break;
-    int u;
-    Cand cd = decode(c, nov, cand_off, cnt, off, lst, ovI, ovJ, u);
-    if (cd.sub < 2) {
-      int v = g.v_off[cd.A] + cd.a, f = g.f_off[cd.B] + cd.b;
-      if (!f_overlap(vb + 6 * v, fb + 6 * f)) continue;
-      d3 v1 = ldX(g.X, nv, v), v0 = ldX(g.Xq, nv, v);
-      int i0 = g.fv[3 * f], i1 = g.fv[3 * f + 1], i2 = g.fv[3 * f + 2];
-      d3 f1[3] = {ldX(g.X, nv, i0), ldX(g.X, nv, i1), ldX(g.X, nv, i2)};
-      d3 f0[3] = {ldX(g.Xq, nv, i0), ldX(g.Xq, nv, i1), ldX(g.Xq, nv, i2)};
-      box bv = box2(v0, v1);
-      box bf = merge(box3(f0[0], f0[1], f0[2]), box3(f1[0], f1[1], f1[2]));
-      if (!overlaps(bv, bf)) continue;
-      tmin = dmin(tmin, pt_collision_time(v0, f0, v1, f1));
-    } else {
-      int ea = g.e_off[cd.A] + cd.a, ebi = g.e_off[cd.B] + cd.b;
-      if (!f_overlap(eb + 6 * ea, eb + 6 * ebi)) continue;
-      int a0 = g.ev[2 * ea], a1 = g.ev[2 * ea + 1], b0 = g.ev[2 * ebi], b1 = g.ev[2 * ebi + 1];
-      d3 A1[2] = {ldX(g.X, nv, a0), ldX(g.X, nv, a1)}, A0[2] = {ldX(g.Xq, nv, a0), ldX(g.Xq, nv, a1)};
-      d3 B1[2] = {ldX(g.X, nv, b0), ldX(g.X, nv, b1)}, B0[2] = {ldX(g.Xq, nv, b0), ldX(g.Xq, nv, b1)};
-      if (!overlaps(box4(A0[0], A0[1], A1[0], A1[1]), box4(B0[0], B0[1], B1[0], B1[1]))) continue;
-      tmin = dmin(tmin, ee_collision_time(A0, B0, A1, B1));
+  for (int sub = 0; sub < 3; ++sub) {
+    int la = sub == 0 ? 0 : (sub == 1 ? 3 : 1);      // vi / vj / ei
+    int lb = sub == 0 ? 5 : (sub == 1 ? 2 : 4);      // fj / fi / ej
+    int A = (sub == 1) ? J : I, B = (sub == 1) ? I : J;
+    int nA = n[la], nB = n[lb];
+    if (nA == 0 || nB == 0) continue;
+    const float* boxA = sub < 2 ? vb : eb;
+    const float* boxB = sub < 2 ? fb : eb;
+    int offA = sub < 2 ? g.v_off[A] : g.e_off[A];
+    int offB = sub < 2 ? g.f_off[B] : g.e_off[B];
+    const int* LA = lst + o[la];
+    const int* LB = lst + o[lb];
+#pragma unroll 1
+    for (int a0 = 0; a0 < nA; a0 += TILE) {
+      int ca = min(TILE, nA - a0);
+#pragma unroll 1
+      for (int b0 = 0; b0 < nB; b0 += TILE) {
+        int cb = min(TILE, nB - b0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < ca; k += NT) {
+          const float* src = boxA + 6 * (offA + LA[a0 + k]);
+          if (MODE == 2) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) sA[6 * k + c] = src[c];
+          } else {
+            finflate(src, ds_f, sA + 6 * k);
+          }
+        }
+        for (int k = threadIdx.x; k < cb; k += NT) {
+          const float* src = boxB + 6 * (offB + LB[b0 + k]);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) sB[6 * k + c] = src[c];
+        }
+        __syncthreads();
+        const int tot = ca * cb;
+#pragma unroll 1
+        for (int k0 = 0; k0 < tot; k0 += NT) {
+          int k = k0 + threadIdx.x;
+          int f = 0;
+          int i = 0, j = 0;
+          if (k < tot) {
+            i = k / cb;
+            j = k - i * cb;
+            const float* a = sA + 6 * i;
+            const float* b = sB + 6 * j;
+            if (a[0] <= b[3] && a[3] >= b[0] && a[1] <= b[4] && a[4] >= b[1] && a[2] <= b[5] && a[5] >= b[2]) {
+              int pa = offA + LA[a0 + i], pb = offB + LB[b0 + j];
+              if (MODE == 2) {
+                tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
+              } else {
+                f = exact_pair(g, P, sub, pa, pb);
+              }
+            }
+          }
+          if (MODE == 0) {
+            if (f) {
+              if (sub < 2) ++run_pt;
+              else ++run_ee;
+            }
+          } else if (MODE == 1) {
+            unsigned m = __ballot_sync(0xffffffffu, f != 0);
+            if (lane == 0) wcnt[w] = __popc(m);
+            __syncthreads();
+            int pre = 0, total = 0;
+#pragma unroll
+            for (int q = 0; q < NT / 32; ++q) {
+              pre += (q < w) ? wcnt[q] : 0;
+              total += wcnt[q];
+            }
+            if (f) {
+              int idx = (sub < 2 ? run_pt : run_ee) + pre + __popc(m & below);
+              int la_id = LA[a0 + i], lb_id = LB[b0 + j];
+              if (sub < 2) {
+                out.pt[4 * idx] = A; out.pt[4 * idx + 1] = la_id; out.pt[4 * idx + 2] = B; out.pt[4 * idx + 3] = lb_id;
+                out.pt_ty[idx] = (int8_t)(f - 1);
+                out.pt_ov[idx] = u;
+              } else {
+                out.ee[4 * idx] = A; out.ee[4 * idx + 1] = la_id; out.ee[4 * idx + 2] = B; out.ee[4 * idx + 3] = lb_id;
+                out.ee_ty[idx] = (int8_t)(f - 1);
+                out.ee_ov[idx] = u;
+              }
+            }
+            if (sub < 2) run_pt += total;
+            else run_ee += total;
+            __syncthreads();
+          }
+        }
+      }
     }
   }
-  if (tmin < 1.0) atomicMin(toi_key, dkey(tmin));
+  if (MODE == 0) {
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) {
+      run_pt += __shfl_xor_sync(0xffffffffu, run_pt, q);
+      run_ee += __shfl_xor_sync(0xffffffffu, run_ee, q);
+    }
+    __shared__ int sp[NT / 32], se[NT / 32];
+    if (lane == 0) {
+      sp[w] = run_pt;
+      se[w] = run_ee;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int a = 0, b = 0;
+      for (int q = 0; q < NT / 32; ++q) {
+        a += sp[q];
+        b += se[q];
+      }
+      ov_npt[u] = a;
+      ov_nee[u] = b;
+    }
+  } else if (MODE == 2) {
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) tmin = dmin(tmin, __shfl_xor_sync(0xffffffffu, tmin, q));
+    if (lane == 0 && tmin < 1.0) atomicMin(toi_key, dkey(tmin));
+  }
 }
 
 // 6a. vertex-ground pairs: flags + per-CTA counts, then ordered write
@@ -606,7 +590,7 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
   cs.fbox.ensure(6 * (size_t)g.nf + 6);
   long long nprim = (long long)g.nv + g.ne + g.nf;
   KLAUNCH(K_PRIM_BOXES, s, k_prim_boxes<<<nblk(nprim, 256), 256, 0, s>>>(g, traj, cs.vbox.p, cs.ebox.p, cs.fbox.p));
-  long long total = 0;
+  int nlst = 0;
   if (nov > 0) {
     cs.bin_cnt.ensure(6 * (size_t)nov + 6);
     cs.bin_off.ensure(6 * (size_t)nov + 6);
@@ -615,22 +599,16 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
                                                         cs.ovcull_f.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.bin_cnt.p,
                                                         nullptr, nullptr));
     scan_exclusive_int(cs.bin_cnt.p, cs.bin_off.p, 6 * nov, d_tot + 2, s, cs.vflag_cnt);
-    cs.cand_cnt.ensure(nov + 1);
-    cs.cand_off.ensure(nov + 2);
-    KLAUNCH(K_CAND_COUNT, s, k_cand_count<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.bin_cnt.p, cs.cand_cnt.p));
-    scan_exclusive_ll(cs.cand_cnt.p, cs.cand_off.p, nov, cs.cand_off.p + nov, s, cs.tmp_ll);
     CK(cudaMemcpyAsync(cs.h_small + 2, d_tot + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(cs.h_ll, cs.cand_off.p + nov, sizeof(long long), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    int nlst = cs.h_small[2];
-    total = cs.h_ll[0];
+    nlst = cs.h_small[2];
     cs.lst.ensure((size_t)nlst + 1);
     KLAUNCH(K_BIN, s, k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, 1, traj, S.ovI.p, S.ovJ.p, cs.ovcull.p,
                                                         cs.ovcull_f.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.bin_cnt.p,
                                                         cs.bin_off.p, cs.lst.p));
   }
   float ds_f = float_round_up(P.d_sqrt);
-  int ntile = (int)((total + NTILE - 1) / NTILE);
+  NarrowOut no{};
   if (traj) {
     cs.toi_key.ensure(2);
     unsigned long long one[2];
@@ -639,10 +617,11 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     memcpy(&b, &o, sizeof(b));
     one[0] = one[1] = b | 0x8000000000000000ull;
     CK(cudaMemcpyAsync(cs.toi_key.p, one, sizeof(one), cudaMemcpyHostToDevice, s));
-    if (total > 0) {
-      prof_work(K_NARROW_TOI, (double)total, 48.0 * g.nv);  // positions at q and q + dq
-      KLAUNCH(K_NARROW_TOI, s, k_narrow_toi<<<ntile, NT, 0, s>>>(g, nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p, S.ovI.p,
-                                        S.ovJ.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.toi_key.p));
+    if (nov > 0) {
+      prof_work(K_NARROW_TOI, nov, 48.0 * g.nv);  // positions at q and q + dq
+      KLAUNCH(K_NARROW_TOI, s, k_narrow_ov<2><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p, cs.bin_off.p,
+                                                                 cs.lst.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, nullptr,
+                                                                 nullptr, nullptr, nullptr, no, cs.toi_key.p));
     }
     if (P.ground && g.nv) {
       KLAUNCH(K_VG_TOI, s, k_vg_toi<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, cs.toi_key.p + 1));
@@ -653,33 +632,33 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     *toi_g = key_to_double(cs.h_toi[1]);
     return;
   }
-  // 5. narrow phase with ordered compaction
+  // 5. narrow phase per overlap: counts, scan, ordered write
   int npt = 0, nee = 0;
-  if (total > 0) {
-    cs.flags.ensure((size_t)total + 1);
-    cs.blk_a.ensure(ntile + 1);
-    cs.blk_b.ensure(ntile + 1);
-    cs.blk_a_off.ensure(ntile + 1);
-    cs.blk_b_off.ensure(ntile + 1);
-    KLAUNCH(K_NARROW_FLAGS, s, k_narrow_flags<<<ntile, NT, 0, s>>>(g, P, ds_f, nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p,
-                                        S.ovI.p, S.ovJ.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.flags.p, cs.blk_a.p,
-                                        cs.blk_b.p));
-    scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, ntile, d_tot + 3, s, cs.vflag_cnt);
-    scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, ntile, d_tot + 4, s, cs.vflag_cnt);
+  if (nov > 0) {
+    cs.blk_a.ensure(nov + 1);
+    cs.blk_b.ensure(nov + 1);
+    cs.blk_a_off.ensure(nov + 1);
+    cs.blk_b_off.ensure(nov + 1);
+    KLAUNCH(K_NARROW_FLAGS, s, k_narrow_ov<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p, cs.bin_off.p,
+                                                                  cs.lst.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.blk_a.p,
+                                                                  cs.blk_b.p, nullptr, nullptr, no, nullptr));
+    scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
+    scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
     CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     npt = cs.h_small[3];
     nee = cs.h_small[4];
-    prof_work(K_NARROW_FLAGS, (double)total, 24.0 * g.nv + 20.0 * ((double)npt + nee));
+    prof_work(K_NARROW_FLAGS, nov, 24.0 * g.nv + 20.0 * ((double)npt + nee));
     S.pt.ensure(4 * (size_t)npt + 4);
     S.pt_ty.ensure(npt + 1);
     S.pt_ov.ensure(npt + 1);
     S.ee.ensure(4 * (size_t)nee + 4);
     S.ee_ty.ensure(nee + 1);
     S.ee_ov.ensure(nee + 1);
-    KLAUNCH(K_NARROW_WRITE, s, k_narrow_write<<<ntile, NT, 0, s>>>(nov, total, cs.cand_off.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p, S.ovI.p,
-                                        S.ovJ.p, cs.flags.p, cs.blk_a_off.p, cs.blk_b_off.p, S.pt.p, S.pt_ty.p,
-                                        S.pt_ov.p, S.ee.p, S.ee_ty.p, S.ee_ov.p));
+    no = NarrowOut{S.pt.p, S.pt_ov.p, S.ee.p, S.ee_ov.p, S.pt_ty.p, S.ee_ty.p};
+    KLAUNCH(K_NARROW_WRITE, s, k_narrow_ov<1><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p, cs.bin_off.p,
+                                                                  cs.lst.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, nullptr,
+                                                                  nullptr, cs.blk_a_off.p, cs.blk_b_off.p, no, nullptr));
   }
   S.npt = npt;
   S.nee = nee;
