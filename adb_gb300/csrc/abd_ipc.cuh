@@ -223,6 +223,228 @@ DEV void psd_project(double (&S)[N][N]) {
     }
 }
 
+// Eigen-projection of a small symmetric matrix held in registers (fully unrolled
+// cyclic Jacobi; N <= 5). Returns whether any eigenvalue was negative (then S holds the
+// projection), leaving S untouched otherwise.
+template <int N>
+DEV bool psd_project_small(double (&S)[N][N]) {
+  double A[N][N], V[N][N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      A[i][j] = S[i][j];
+      V[i][j] = (i == j) ? 1.0 : 0.0;
+    }
+  for (int sweep = 0; sweep < 20; ++sweep) {
+    double off = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        double v = A[i][j] * A[i][j];
+        tot += v;
+        if (i != j) off += v;
+      }
+    if (off <= 1e-32 * tot || off == 0.0) break;
+#pragma unroll
+    for (int p = 0; p < N - 1; ++p)
+#pragma unroll
+      for (int q = p + 1; q < N; ++q) {
+        double apq = A[p][q];
+        if (apq != 0.0) {
+          double theta = (A[q][q] - A[p][p]) / (2 * apq);
+          double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
+          double c = 1 / sqrt(t * t + 1), s = t * c;
+#pragma unroll
+          for (int k = 0; k < N; ++k) {
+            double akp = A[k][p], akq = A[k][q];
+            A[k][p] = c * akp - s * akq;
+            A[k][q] = s * akp + c * akq;
+          }
+#pragma unroll
+          for (int k = 0; k < N; ++k) {
+            double apk = A[p][k], aqk = A[q][k];
+            A[p][k] = c * apk - s * aqk;
+            A[q][k] = s * apk + c * aqk;
+          }
+#pragma unroll
+          for (int k = 0; k < N; ++k) {
+            double vkp = V[k][p], vkq = V[k][q];
+            V[k][p] = c * vkp - s * vkq;
+            V[k][q] = s * vkp + c * vkq;
+          }
+          A[p][q] = 0.0;
+          A[q][p] = 0.0;
+        }
+      }
+  }
+  bool neg = false;
+  double lam[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    lam[i] = A[i][i];
+    neg |= lam[i] < 0.0;
+  }
+  if (!neg) return false;
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double acc = 0;
+#pragma unroll
+      for (int k = 0; k < N; ++k) acc += lam[k] > 0 ? V[i][k] * lam[k] * V[j][k] : 0.0;
+      S[i][j] = acc;
+    }
+  return true;
+}
+
+// Reduced projection of a non-mollified pair: H lives in the span of
+// { c (x) e_x, c (x) e_y, c (x) e_z, a_k' (x) w } (a_k' = the parameter directions
+// orthonormalised against c; at most 3 + m <= 5 columns), where
+//   S_r = [[2 b' |c|^2 I + 4 b'' |c|^2 w w^T, 0], [0, 0]] - b' Phi_r G^-1 Phi_r^T.
+// S_r is projected (analytically for m = 0) and written back in the 9-dim Q (x) I basis.
+template <int M>
+DEV void reduced_project(const Stencil& st, d3 w, const d3* W, const double (&Gi)[2][2], double B1, double B2,
+                         bool psd, double (&S9)[9][9]) {
+  constexpr int N = 3 + M;
+  double cn2 = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) cn2 += st.c[i] * st.c[i];
+  double cn = sqrt(cn2);
+  double ch[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) ch[i] = st.c[i] / cn;
+  double wn = sqrt(fdot(w, w));
+  d3 wh = fscl(1.0 / wn, w);
+  // orthonormal parameter directions a_hat (R^4, _|_ c)
+  double ah[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  double ca[2] = {0, 0};   // c_hat . a_k
+  double aa[2][2] = {{0, 0}, {0, 0}};  // a_hat_l . a_k
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    double t[4];
+    double d = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) d += ch[i] * st.a[k][i];
+    ca[k] = d;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) t[i] = st.a[k][i] - d * ch[i];
+#pragma unroll
+    for (int l = 0; l < k; ++l) {
+      double e = 0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) e += ah[l][i] * t[i];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) t[i] -= e * ah[l][i];
+    }
+    double tn = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) tn += t[i] * t[i];
+    tn = 1.0 / sqrt(tn);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) ah[k][i] = t[i] * tn;
+  }
+#pragma unroll
+  for (int l = 0; l < M; ++l)
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      double e = 0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) e += ah[l][i] * st.a[k][i];
+      aa[l][k] = e;
+    }
+  double Sr[N][N];
+  double wv[3] = {w.x, w.y, w.z};
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < N; ++j) Sr[i][j] = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Sr[i][j] = (i == j ? 2 * B1 * cn2 : 0.0) + 4 * B2 * cn2 * wv[i] * wv[j];
+  if (M > 0) {
+    double Phi[N][M > 0 ? M : 1];
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      double Wk[3] = {W[k].x, W[k].y, W[k].z};
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Phi[j][k] = 2 * (cn * Wk[j] + ca[k] * wv[j]);
+#pragma unroll
+      for (int l = 0; l < M; ++l) Phi[3 + l][k] = 2 * aa[l][k] * wn;
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        double acc = 0;
+#pragma unroll
+        for (int k = 0; k < M; ++k)
+#pragma unroll
+          for (int l = 0; l < M; ++l) acc += Phi[i][k] * Gi[k][l] * Phi[j][l];
+        Sr[i][j] -= B1 * acc;
+      }
+  }
+  if (psd) {
+    if (M == 0) {
+      // eigenpairs: w_hat with 2b'|c|^2 + 4b''|c|^2 |w|^2, the two normals with 2b'|c|^2
+      double lw = 2 * B1 * cn2 + 4 * B2 * cn2 * wn * wn, ln = 2 * B1 * cn2;
+      if (lw < 0.0 || ln < 0.0) {
+        double whv[3] = {wh.x, wh.y, wh.z};
+        double lwp = lw > 0 ? lw : 0.0, lnp = ln > 0 ? ln : 0.0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) Sr[i][j] = lnp * (i == j ? 1.0 : 0.0) + (lwp - lnp) * whv[i] * whv[j];
+      }
+    } else {
+      psd_project_small<N>(Sr);
+    }
+  }
+  // back to the 9-dim basis: column alpha of the reduced basis has Q-coordinates
+  // (Q^T u_alpha) (x) v_alpha
+  double Bq[9][N];
+  double cq[3];
+  qt4(ch, cq);
+  double whv[3] = {wh.x, wh.y, wh.z};
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Bq[3 * a + r][j] = (r == j) ? cq[a] : 0.0;
+    }
+#pragma unroll
+  for (int l = 0; l < M; ++l) {
+    double aq[3];
+    qt4(ah[l], aq);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) Bq[3 * a + r][3 + l] = aq[a] * whv[r];
+  }
+  double T[9][N];
+#pragma unroll
+  for (int p = 0; p < 9; ++p)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double acc = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) acc += Bq[p][i] * Sr[i][j];
+      T[p][j] = acc;
+    }
+#pragma unroll
+  for (int p = 0; p < 9; ++p)
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      double acc = 0;
+#pragma unroll
+      for (int j = 0; j < N; ++j) acc += T[p][j] * Bq[q][j];
+      S9[p][q] = acc;
+    }
+}
+
 // Friction stencil of a pair: tangent basis (c0, c1), relative-displacement weights
 // gamma (model/pt_ipc.cpp:22-107, model/ee_ipc.cpp:21-118).
 struct FrictionFrame {
@@ -431,6 +653,14 @@ DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& b
           Hx[3 + i][j] = 2.0 * hvu;
         }
     }
+  }
+  if (!mollified) {
+    if (st.m == 0) reduced_project<0>(st, w, W, Gi, B1, B2, psd, S);
+    else if (st.m == 1) reduced_project<1>(st, w, W, Gi, B1, B2, psd, S);
+    else reduced_project<2>(st, w, W, Gi, B1, B2, psd, S);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) g[i] = fscl(B1 * 2 * st.c[i], w);
+    return;
   }
   for (int p = 0; p < 9; ++p)
     for (int q = 0; q < 9; ++q) {

@@ -306,145 +306,200 @@ struct NarrowOut {
   int8_t *pt_ty, *ee_ty;
 };
 
-// 5. Narrow phase, one CTA per overlap. For each of the three sub-problems
-// (v(I) x f(J), v(J) x f(I), e(I) x e(J)) the float boxes of both lists are staged in
-// shared memory (chunks of TILE), every (i, j) is tested in row-major order with the
-// outward-rounded float boxes, and the survivors get the exact test.
-// MODE 0: per-overlap PT/EE counts; MODE 1: ordered write at the scanned offsets;
-// MODE 2: trajectory TOI (atomic min).
+struct SubLists {
+  int A, B, nA, nB, offA, offB;
+  const int *LA, *LB;
+  const float *boxA, *boxB;
+};
+
+__device__ __forceinline__ SubLists sub_lists(const Geo& g, int sub, int I, int J, const int* n, const int* o,
+                                              const int* lst, const float* vb, const float* eb, const float* fb) {
+  SubLists L;
+  int la = sub == 0 ? 0 : (sub == 1 ? 3 : 1);  // vi / vj / ei
+  int lb = sub == 0 ? 5 : (sub == 1 ? 2 : 4);  // fj / fi / ej
+  L.A = (sub == 1) ? J : I;
+  L.B = (sub == 1) ? I : J;
+  L.nA = n[la];
+  L.nB = n[lb];
+  L.boxA = sub < 2 ? vb : eb;
+  L.boxB = sub < 2 ? fb : eb;
+  L.offA = sub < 2 ? g.v_off[L.A] : g.e_off[L.A];
+  L.offB = sub < 2 ? g.f_off[L.B] : g.e_off[L.B];
+  L.LA = lst + o[la];
+  L.LB = lst + o[lb];
+  return L;
+}
+
+// Stages one chunk of each list's float boxes in shared memory (A side inflated by
+// sqrt(dhat), rounded outward, unless `traj`).
+__device__ __forceinline__ void stage(const SubLists& L, int a0, int ca, int b0, int cb, bool inflate_a, float ds_f,
+                                      float* sA, float* sB) {
+  __syncthreads();
+  for (int k = threadIdx.x; k < ca; k += blockDim.x) {
+    const float* src = L.boxA + 6 * (L.offA + L.LA[a0 + k]);
+    if (inflate_a) finflate(src, ds_f, sA + 6 * k);
+    else
+#pragma unroll
+      for (int c = 0; c < 6; ++c) sA[6 * k + c] = src[c];
+  }
+  for (int k = threadIdx.x; k < cb; k += blockDim.x) {
+    const float* src = L.boxB + 6 * (L.offB + L.LB[b0 + k]);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sB[6 * k + c] = src[c];
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool f_hit(const float* a, const float* b) {
+  return a[0] <= b[3] && a[3] >= b[0] && a[1] <= b[4] && a[4] >= b[1] && a[2] <= b[5] && a[5] >= b[2];
+}
+
+// 5a. Narrow phase, one CTA per overlap, count (MODE 0) or trajectory TOI (MODE 2).
+// For each sub-problem (v(I) x f(J), v(J) x f(I), e(I) x e(J)) the float boxes of both
+// lists are staged in shared memory; each thread keeps one A box in registers and walks
+// the B boxes (a shared-memory broadcast per step); survivors get the exact test.
 template <int MODE>
-__global__ void __launch_bounds__(NT) k_narrow_ov(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
-                                                  const int* cnt, const int* off, const int* lst, const float* vb,
-                                                  const float* eb, const float* fb, int* ov_npt, int* ov_nee,
-                                                  const int* ov_pt_off, const int* ov_ee_off, NarrowOut out,
-                                                  unsigned long long* toi_key) {
+__global__ void __launch_bounds__(NT) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
+                                                    const int* cnt, const int* off, const int* lst, const float* vb,
+                                                    const float* eb, const float* fb, int* sub_cnt,
+                                                    unsigned long long* toi_key) {
   __shared__ float sA[TILE * 6], sB[TILE * 6];
-  __shared__ int wcnt[NT / 32];
   const int u = blockIdx.x;
-  const int I = ovI[u], J = ovJ[u];
   const int* n = cnt + 6 * u;
   const int* o = off + 6 * u;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const unsigned below = (1u << lane) - 1u;
-  int run_pt = (MODE == 1) ? ov_pt_off[u] : 0, run_ee = (MODE == 1) ? ov_ee_off[u] : 0;
+  int c3s[3] = {0, 0, 0};
   double tmin = 1.0;
 #pragma unroll 1
   for (int sub = 0; sub < 3; ++sub) {
-    int la = sub == 0 ? 0 : (sub == 1 ? 3 : 1);      // vi / vj / ei
-    int lb = sub == 0 ? 5 : (sub == 1 ? 2 : 4);      // fj / fi / ej
-    int A = (sub == 1) ? J : I, B = (sub == 1) ? I : J;
-    int nA = n[la], nB = n[lb];
-    if (nA == 0 || nB == 0) continue;
-    const float* boxA = sub < 2 ? vb : eb;
-    const float* boxB = sub < 2 ? fb : eb;
-    int offA = sub < 2 ? g.v_off[A] : g.e_off[A];
-    int offB = sub < 2 ? g.f_off[B] : g.e_off[B];
-    const int* LA = lst + o[la];
-    const int* LB = lst + o[lb];
+    SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, o, lst, vb, eb, fb);
+    if (L.nA == 0 || L.nB == 0) continue;
+    int cs = 0;
 #pragma unroll 1
-    for (int a0 = 0; a0 < nA; a0 += TILE) {
-      int ca = min(TILE, nA - a0);
+    for (int a0 = 0; a0 < L.nA; a0 += TILE) {
+      int ca = min(TILE, L.nA - a0);
 #pragma unroll 1
-      for (int b0 = 0; b0 < nB; b0 += TILE) {
-        int cb = min(TILE, nB - b0);
-        __syncthreads();
-        for (int k = threadIdx.x; k < ca; k += NT) {
-          const float* src = boxA + 6 * (offA + LA[a0 + k]);
-          if (MODE == 2) {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) sA[6 * k + c] = src[c];
-          } else {
-            finflate(src, ds_f, sA + 6 * k);
-          }
-        }
-        for (int k = threadIdx.x; k < cb; k += NT) {
-          const float* src = boxB + 6 * (offB + LB[b0 + k]);
-#pragma unroll
-          for (int c = 0; c < 6; ++c) sB[6 * k + c] = src[c];
-        }
-        __syncthreads();
-        const int tot = ca * cb;
+      for (int b0 = 0; b0 < L.nB; b0 += TILE) {
+        int cb = min(TILE, L.nB - b0);
+        stage(L, a0, ca, b0, cb, MODE != 2, ds_f, sA, sB);
+        // thread t: row i = t mod ca, columns j = t / ca + q * (NT / ca) (rows >= NT: stride)
+        int phases = ca >= NT ? 1 : NT / ca;
+        int row0 = threadIdx.x % (ca < NT ? ca : NT);
+        int ph = ca < NT ? threadIdx.x / ca : 0;
+        if (ph < phases) {
 #pragma unroll 1
-        for (int k0 = 0; k0 < tot; k0 += NT) {
-          int k = k0 + threadIdx.x;
-          int f = 0;
-          int i = 0, j = 0;
-          if (k < tot) {
-            i = k / cb;
-            j = k - i * cb;
-            const float* a = sA + 6 * i;
-            const float* b = sB + 6 * j;
-            if (a[0] <= b[3] && a[3] >= b[0] && a[1] <= b[4] && a[4] >= b[1] && a[2] <= b[5] && a[5] >= b[2]) {
-              int pa = offA + LA[a0 + i], pb = offB + LB[b0 + j];
-              if (MODE == 2) {
-                tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
-              } else {
-                f = exact_pair(g, P, sub, pa, pb);
-              }
-            }
-          }
-          if (MODE == 0) {
-            if (f) {
-              if (sub < 2) ++run_pt;
-              else ++run_ee;
-            }
-          } else if (MODE == 1) {
-            unsigned m = __ballot_sync(0xffffffffu, f != 0);
-            if (lane == 0) wcnt[w] = __popc(m);
-            __syncthreads();
-            int pre = 0, total = 0;
+          for (int i = row0; i < ca; i += (ca < NT ? ca : NT)) {
+            float a[6];
 #pragma unroll
-            for (int q = 0; q < NT / 32; ++q) {
-              pre += (q < w) ? wcnt[q] : 0;
-              total += wcnt[q];
+            for (int c = 0; c < 6; ++c) a[c] = sA[6 * i + c];
+            int pa = L.offA + L.LA[a0 + i];
+#pragma unroll 1
+            for (int j = ph; j < cb; j += phases) {
+              if (!f_hit(a, sB + 6 * j)) continue;
+              int pb = L.offB + L.LB[b0 + j];
+              if (MODE == 2) tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
+              else cs += exact_pair(g, P, sub, pa, pb) != 0;
             }
-            if (f) {
-              int idx = (sub < 2 ? run_pt : run_ee) + pre + __popc(m & below);
-              int la_id = LA[a0 + i], lb_id = LB[b0 + j];
-              if (sub < 2) {
-                out.pt[4 * idx] = A; out.pt[4 * idx + 1] = la_id; out.pt[4 * idx + 2] = B; out.pt[4 * idx + 3] = lb_id;
-                out.pt_ty[idx] = (int8_t)(f - 1);
-                out.pt_ov[idx] = u;
-              } else {
-                out.ee[4 * idx] = A; out.ee[4 * idx + 1] = la_id; out.ee[4 * idx + 2] = B; out.ee[4 * idx + 3] = lb_id;
-                out.ee_ty[idx] = (int8_t)(f - 1);
-                out.ee_ov[idx] = u;
-              }
-            }
-            if (sub < 2) run_pt += total;
-            else run_ee += total;
-            __syncthreads();
           }
         }
       }
     }
+    c3s[sub] = cs;
   }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (MODE == 0) {
+    __shared__ int sh[3][NT / 32];
 #pragma unroll
-    for (int q = 16; q > 0; q >>= 1) {
-      run_pt += __shfl_xor_sync(0xffffffffu, run_pt, q);
-      run_ee += __shfl_xor_sync(0xffffffffu, run_ee, q);
-    }
-    __shared__ int sp[NT / 32], se[NT / 32];
-    if (lane == 0) {
-      sp[w] = run_pt;
-      se[w] = run_ee;
+    for (int k = 0; k < 3; ++k) {
+      int v = c3s[k];
+#pragma unroll
+      for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(0xffffffffu, v, q);
+      if (lane == 0) sh[k][w] = v;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int a = 0, b = 0;
-      for (int q = 0; q < NT / 32; ++q) {
-        a += sp[q];
-        b += se[q];
-      }
-      ov_npt[u] = a;
-      ov_nee[u] = b;
+    if (threadIdx.x < 3) {
+      int t = 0;
+      for (int q = 0; q < NT / 32; ++q) t += sh[threadIdx.x][q];
+      sub_cnt[3 * u + threadIdx.x] = t;
     }
-  } else if (MODE == 2) {
+  } else {
 #pragma unroll
     for (int q = 16; q > 0; q >>= 1) tmin = dmin(tmin, __shfl_xor_sync(0xffffffffu, tmin, q));
     if (lane == 0 && tmin < 1.0) atomicMin(toi_key, dkey(tmin));
   }
+}
+
+// 5b. Ordered write. Sub-problems without pairs are skipped; each (i, j) chunk is walked
+// in row-major order with a CTA-wide ordered compaction, stopping once the sub-problem's
+// count (from the count pass) has been written.
+__global__ void __launch_bounds__(NT) k_narrow_write(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
+                                                     const int* cnt, const int* off, const int* lst, const float* vb,
+                                                     const float* eb, const float* fb, const int* sub_cnt,
+                                                     const int* ov_pt_off, const int* ov_ee_off, NarrowOut out) {
+  __shared__ float sA[TILE * 6], sB[TILE * 6];
+  __shared__ int wcnt[NT / 32];
+  const int u = blockIdx.x;
+  const int* sc = sub_cnt + 3 * u;
+  if (sc[0] + sc[1] + sc[2] == 0) return;
+  const int* n = cnt + 6 * u;
+  const int* o = off + 6 * u;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  int run_pt = ov_pt_off[u], run_ee = ov_ee_off[u];
+#pragma unroll 1
+  for (int sub = 0; sub < 3; ++sub) {
+    if (sc[sub] == 0) continue;
+    SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, o, lst, vb, eb, fb);
+    int need = sc[sub], done = 0;
+#pragma unroll 1
+    for (int a0 = 0; a0 < L.nA && done < need; a0 += TILE) {
+      int ca = min(TILE, L.nA - a0);
+#pragma unroll 1
+      for (int b0 = 0; b0 < L.nB && done < need; b0 += TILE) {
+        int cb = min(TILE, L.nB - b0);
+        stage(L, a0, ca, b0, cb, true, ds_f, sA, sB);
+        const int tot = ca * cb;
+#pragma unroll 1
+        for (int k0 = 0; k0 < tot && done < need; k0 += NT) {
+          int k = k0 + threadIdx.x;
+          int f = 0, i = 0, j = 0;
+          if (k < tot) {
+            i = k / cb;
+            j = k - i * cb;
+            if (f_hit(sA + 6 * i, sB + 6 * j))
+              f = exact_pair(g, P, sub, L.offA + L.LA[a0 + i], L.offB + L.LB[b0 + j]);
+          }
+          unsigned m = __ballot_sync(0xffffffffu, f != 0);
+          if (lane == 0) wcnt[w] = __popc(m);
+          __syncthreads();
+          int pre = 0, total = 0;
+#pragma unroll
+          for (int q = 0; q < NT / 32; ++q) {
+            pre += (q < w) ? wcnt[q] : 0;
+            total += wcnt[q];
+          }
+          if (f) {
+            int idx = (sub < 2 ? run_pt : run_ee) + pre + __popc(m & below);
+            int la_id = L.LA[a0 + i], lb_id = L.LB[b0 + j];
+            int* dst = sub < 2 ? out.pt : out.ee;
+            dst[4 * idx] = L.A; dst[4 * idx + 1] = la_id; dst[4 * idx + 2] = L.B; dst[4 * idx + 3] = lb_id;
+            (sub < 2 ? out.pt_ty : out.ee_ty)[idx] = (int8_t)(f - 1);
+            (sub < 2 ? out.pt_ov : out.ee_ov)[idx] = u;
+          }
+          if (sub < 2) run_pt += total;
+          else run_ee += total;
+          done += total;
+          __syncthreads();
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_sub_totals(int nov, const int* sub_cnt, int* npt, int* nee) {
+  int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nov) return;
+  npt[u] = sub_cnt[3 * u] + sub_cnt[3 * u + 1];
+  nee[u] = sub_cnt[3 * u + 2];
 }
 
 // 6a. vertex-ground pairs: flags + per-CTA counts, then ordered write
@@ -619,9 +674,9 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     CK(cudaMemcpyAsync(cs.toi_key.p, one, sizeof(one), cudaMemcpyHostToDevice, s));
     if (nov > 0) {
       prof_work(K_NARROW_TOI, nov, 48.0 * g.nv);  // positions at q and q + dq
-      KLAUNCH(K_NARROW_TOI, s, k_narrow_ov<2><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p, cs.bin_off.p,
-                                                                 cs.lst.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, nullptr,
-                                                                 nullptr, nullptr, nullptr, no, cs.toi_key.p));
+      KLAUNCH(K_NARROW_TOI, s, k_narrow_scan<2><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
+                                                                   cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
+                                                                   cs.fbox.p, nullptr, cs.toi_key.p));
     }
     if (P.ground && g.nv) {
       KLAUNCH(K_VG_TOI, s, k_vg_toi<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, cs.toi_key.p + 1));
@@ -639,9 +694,11 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     cs.blk_b.ensure(nov + 1);
     cs.blk_a_off.ensure(nov + 1);
     cs.blk_b_off.ensure(nov + 1);
-    KLAUNCH(K_NARROW_FLAGS, s, k_narrow_ov<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p, cs.bin_off.p,
-                                                                  cs.lst.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.blk_a.p,
-                                                                  cs.blk_b.p, nullptr, nullptr, no, nullptr));
+    cs.sub_cnt.ensure(3 * (size_t)nov + 3);
+    KLAUNCH(K_NARROW_FLAGS, s, k_narrow_scan<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
+                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
+                                                                    cs.fbox.p, cs.sub_cnt.p, nullptr));
+    KLAUNCH(K_NARROW_FLAGS, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
     scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
     scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
     CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -656,9 +713,10 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     S.ee_ty.ensure(nee + 1);
     S.ee_ov.ensure(nee + 1);
     no = NarrowOut{S.pt.p, S.pt_ov.p, S.ee.p, S.ee_ov.p, S.pt_ty.p, S.ee_ty.p};
-    KLAUNCH(K_NARROW_WRITE, s, k_narrow_ov<1><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p, cs.bin_off.p,
-                                                                  cs.lst.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, nullptr,
-                                                                  nullptr, cs.blk_a_off.p, cs.blk_b_off.p, no, nullptr));
+    KLAUNCH(K_NARROW_WRITE, s, k_narrow_write<<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
+                                                                  cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
+                                                                  cs.fbox.p, cs.sub_cnt.p, cs.blk_a_off.p,
+                                                                  cs.blk_b_off.p, no));
   }
   S.npt = npt;
   S.nee = nee;

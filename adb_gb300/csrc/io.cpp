@@ -230,7 +230,7 @@ extern "C" int abd_create_from_files(const char* config_json, const char* scene_
   c.max_uk = pd ? pd->num("max_uk", 0.0) : 0.0;
   c.gravity_y = cfgj.flag("gravity", true) ? -9.8 : 0.0;
   c.ls_grad_tol = 1e-3;
-  c.pcg_rel_tol = cfgj.num("pcg_rel_tol", 1e-12);
+  c.pcg_rel_tol = cfgj.num("pcg_rel_tol", 1e-14);
   c.max_iter = (int)cfgj.num("max_iter", 1000);
   c.ground = cfgj.flag("ground", true);
   c.pt = cfgj.flag("pt", true);
@@ -242,7 +242,7 @@ extern "C" int abd_create_from_files(const char* config_json, const char* scene_
   c.pt_fric = cfgj.flag("pt_friction", true);
   c.ee_fric = cfgj.flag("ee_friction", true);
   c.clip = pi ? (int)pi->num("clip", 0) : 0;
-  c.pcg_max_iter = (int)cfgj.num("pcg_max_iter", 2000);
+  c.pcg_max_iter = (int)cfgj.num("pcg_max_iter", 5000);
 
   std::string dir = scene_json;
   size_t sl = dir.find_last_of('/');

@@ -59,8 +59,8 @@ class Config:
     clip: int = 0                  # params_int.clip
     iaabb: int = 3
     # GPU solver controls (no reference counterpart: the reference factorizes directly)
-    pcg_rel_tol: float = 1e-12
-    pcg_max_iter: int = 2000
+    pcg_rel_tol: float = 1e-14
+    pcg_max_iter: int = 5000
 
     @property
     def gravity_y(self) -> float:
