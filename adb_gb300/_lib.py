@@ -82,6 +82,9 @@ def lib():
         L.abd_profile.argtypes = [H, C.c_int]
         L.abd_kernel_times.argtypes = [H, C.c_int, C.c_char_p, _D, C.POINTER(C.c_longlong)]
         L.abd_kernel_work.argtypes = [H, C.c_int, C.c_char_p, _D, C.POINTER(C.c_longlong), _D, _D]
+        L.abd_pt_min_toi_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.abd_noalloc_last_error.restype = C.c_char_p
+        L.abd_noalloc_last_error.argtypes = []
         L.abd_measure_fp64_gflops.restype = C.c_double
         L.abd_measure_fp64_gflops.argtypes = []
         _lib = L
@@ -93,7 +96,7 @@ EXPORTED = ["abd_create", "abd_create_from_files", "abd_step", "abd_get_state", 
             "abd_get_iter", "abd_set_iter", "abd_last_error", "abd_destroy", "abd_profile", "abd_kernel_times", "abd_kernel_work", "abd_cull", "abd_get_pairs",
             "abd_newton_system", "abd_newton_dq", "abd_ipc_hess_pt_batch", "abd_ipc_hess_ee_batch",
             "abd_pt_collision_time_batch", "abd_ee_collision_time_batch", "abd_pt_distance_batch",
-            "abd_ee_distance_batch", "abd_measure_fp64_gflops"]
+            "abd_ee_distance_batch", "abd_pt_min_toi_noalloc", "abd_noalloc_last_error", "abd_measure_fp64_gflops"]
 
 
 def dptr(a):

@@ -144,6 +144,20 @@ int abd_ee_collision_time_batch(int n, const double* x, double* toi);
 int abd_pt_distance_batch(int n, const double* x, int* type, double* dist);
 int abd_ee_distance_batch(int n, const double* x, int* type, double* dist);
 
+/* Allocation-free minimum point-triangle time of impact. No counterpart in the
+ * reference. For callers that cannot allocate device memory where they call it (inside
+ * a CUDA-graph stream capture, or under a host framework whose pool allocator owns all
+ * device memory): inputs and outputs are the caller's device buffers -- d_x (n * 24
+ * doubles, as abd_pt_collision_time_batch), d_toi (n per-trajectory TOIs), d_min (the
+ * minimum) -- and the only scratch is a fixed 256 kB array in this library's device
+ * memory, shared by all calls (overlapping calls on the GPU race; serialise them).
+ * n <= ABD_NOALLOC_MAX_N, else ABD_ERR_INVALID. The first call on each device looks the
+ * scratch address up and must come before any stream capture. Work is queued on
+ * `stream` (a cudaStream_t, NULL = default stream); the call does not synchronise. */
+#define ABD_NOALLOC_MAX_N (1 << 22)
+int abd_pt_min_toi_noalloc(int n, const double* d_x, double* d_toi, double* d_min, void* stream);
+const char* abd_noalloc_last_error(void);
+
 /* Dense FP64 FMA throughput of this GPU in GFLOP/s (roofline denominator for the
  * FP64-bound kernels; measured with a fixed independent-FMA kernel). */
 double abd_measure_fp64_gflops(void);
