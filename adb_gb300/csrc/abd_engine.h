@@ -90,7 +90,9 @@ struct CullScratch {
   DBuf<long long> cand_cnt, cand_off;
   DBuf<uint8_t> flags;
   DBuf<int> blk_a, blk_b, blk_a_off, blk_b_off;
-  DBuf<int> vflag_cnt, vflag_off, sub_cnt;
+  DBuf<int> vflag_cnt, vflag_off, sub_cnt, stage_off;
+  DBuf<unsigned long long> stage_key;   // sorted accepted pairs per overlap (sub, i, j)
+  DBuf<int8_t> stage_ty;
   DBuf<unsigned long long> toi_key;     // [0] pt/ee, [1] ground
   DBuf<int> tmp_int;
   DBuf<long long> tmp_ll;

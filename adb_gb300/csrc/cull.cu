@@ -250,7 +250,8 @@ __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const 
 }
 
 constexpr int NT = 256;     // narrow-phase threads per CTA
-constexpr int TILE = 1000;  // primitives of one list staged in shared memory (2 x 24 kB)
+constexpr int TILE = 512;   // primitives of one list staged in shared memory (2 x 12 kB)
+constexpr int REC_CAP = 2048;  // accepted pairs of one overlap kept in shared memory for sorting
 
 __device__ __forceinline__ void finflate(const float* s, float ds, float* o) {
   o[0] = __fsub_rd(s[0], ds); o[1] = __fsub_rd(s[1], ds); o[2] = __fsub_rd(s[2], ds);
@@ -273,12 +274,14 @@ __device__ __forceinline__ int exact_pair(const Geo& g, const Params& P, int sub
     box bv = inflate(box{p, p}, P.d_sqrt);
     d3 t0 = ldX(g.X, nv, g.fv[3 * pb]), t1 = ldX(g.X, nv, g.fv[3 * pb + 1]), t2 = ldX(g.X, nv, g.fv[3 * pb + 2]);
     if (!overlaps(bv, box3(t0, t1, t2))) return 0;
+    if (lb_reject_pt(p, t0, t1, t2, P.dhat)) return 0;
     int ty = pt_type(p, t0, t1, t2);
     return (pt_dist(p, t0, t1, t2, ty) < P.dhat) ? 1 + ty : 0;
   }
   d3 a0 = ldX(g.X, nv, g.ev[2 * pa]), a1 = ldX(g.X, nv, g.ev[2 * pa + 1]);
   d3 b0 = ldX(g.X, nv, g.ev[2 * pb]), b1 = ldX(g.X, nv, g.ev[2 * pb + 1]);
   if (!overlaps(inflate(box2(a0, a1), P.d_sqrt), box2(b0, b1))) return 0;
+  if (lb_reject_ee(a0, a1, b0, b1, P.dhat)) return 0;
   int ty = ee_type(a0, a1, b0, b1);
   return (ee_dist(a0, a1, b0, b1, ty) < P.dhat) ? 1 + ty : 0;
 }
@@ -362,13 +365,19 @@ template <int MODE>
 __global__ void __launch_bounds__(NT) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
                                                     const int* cnt, const int* off, const int* lst, const float* vb,
                                                     const float* eb, const float* fb, int* sub_cnt,
-                                                    unsigned long long* toi_key) {
+                                                    unsigned long long* toi_key, unsigned long long* stage_key,
+                                                    int8_t* stage_ty, int* stage_off, int* stage_total,
+                                                    int stage_cap) {
   __shared__ float sA[TILE * 6], sB[TILE * 6];
+  __shared__ unsigned long long recK[MODE == 0 ? REC_CAP : 1];
+  __shared__ int8_t recT[MODE == 0 ? REC_CAP : 1];
+  __shared__ int rec_n, rec_base;
   const int u = blockIdx.x;
   const int* n = cnt + 6 * u;
   const int* o = off + 6 * u;
   int c3s[3] = {0, 0, 0};
   double tmin = 1.0;
+  if (MODE == 0 && threadIdx.x == 0) rec_n = 0;
 #pragma unroll 1
   for (int sub = 0; sub < 3; ++sub) {
     SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, o, lst, vb, eb, fb);
@@ -396,8 +405,20 @@ __global__ void __launch_bounds__(NT) k_narrow_scan(Geo g, Params P, float ds_f,
             for (int j = ph; j < cb; j += phases) {
               if (!f_hit(a, sB + 6 * j)) continue;
               int pb = L.offB + L.LB[b0 + j];
-              if (MODE == 2) tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
-              else cs += exact_pair(g, P, sub, pa, pb) != 0;
+              if (MODE == 2) {
+                tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
+              } else {
+                int f = exact_pair(g, P, sub, pa, pb);
+                if (f) {
+                  ++cs;
+                  int slot = atomicAdd(&rec_n, 1);
+                  if (slot < REC_CAP) {
+                    recK[slot] = ((unsigned long long)sub << 60) | ((unsigned long long)(a0 + i) << 30) |
+                                 (unsigned long long)(b0 + j);
+                    recT[slot] = (int8_t)(f - 1);
+                  }
+                }
+              }
             }
           }
         }
@@ -421,10 +442,83 @@ __global__ void __launch_bounds__(NT) k_narrow_scan(Geo g, Params P, float ds_f,
       for (int q = 0; q < NT / 32; ++q) t += sh[threadIdx.x][q];
       sub_cnt[3 * u + threadIdx.x] = t;
     }
+    // Sort the collected (sub, i, j) keys (bitonic, shared memory) and stage them, so
+    // the write pass only copies. Overlaps with more pairs than REC_CAP are marked
+    // (stage_off = -1) and written by the recomputing pass instead.
+    int nr = rec_n;
+    if (nr > REC_CAP || nr == 0) {
+      if (threadIdx.x == 0) stage_off[u] = (nr == 0) ? 0 : -1;
+      return;
+    }
+    int np2 = 1;
+    while (np2 < nr) np2 <<= 1;
+    for (int k = nr + threadIdx.x; k < np2; k += NT) recK[k] = ~0ull;
+    __syncthreads();
+    for (int size = 2; size <= np2; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int t = threadIdx.x; t < (np2 >> 1); t += NT) {
+          int lo = 2 * t - (t & (stride - 1));
+          int hi = lo + stride;
+          bool up = ((lo & size) == 0);
+          unsigned long long a = recK[lo], b = recK[hi];
+          if ((a > b) == up) {
+            recK[lo] = b;
+            recK[hi] = a;
+            int8_t ta = recT[lo];
+            recT[lo] = recT[hi];
+            recT[hi] = ta;
+          }
+        }
+        __syncthreads();
+      }
+    if (threadIdx.x == 0) {
+      int base = atomicAdd(stage_total, nr);
+      rec_base = (base + nr <= stage_cap) ? base : -2;
+      stage_off[u] = rec_base;
+    }
+    __syncthreads();
+    if (rec_base >= 0)
+      for (int k = threadIdx.x; k < nr; k += NT) {
+        stage_key[rec_base + k] = recK[k];
+        stage_ty[rec_base + k] = recT[k];
+      }
   } else {
 #pragma unroll
     for (int q = 16; q > 0; q >>= 1) tmin = dmin(tmin, __shfl_xor_sync(0xffffffffu, tmin, q));
     if (lane == 0 && tmin < 1.0) atomicMin(toi_key, dkey(tmin));
+  }
+}
+
+// 5b'. Copy of the staged, sorted pairs of each overlap to their final slots.
+__global__ void k_narrow_copy(int nov, const int* ovI, const int* ovJ, const int* off, const int* lst,
+                              const int* sub_cnt, const unsigned long long* stage_key, const int8_t* stage_ty,
+                              const int* stage_off, const int* ov_pt_off, const int* ov_ee_off, NarrowOut out) {
+  int u = blockIdx.x;
+  if (u >= nov) return;
+  const int* sc = sub_cnt + 3 * u;
+  int nr = sc[0] + sc[1] + sc[2];
+  int so = stage_off[u];
+  if (nr == 0 || so < 0) return;
+  int I = ovI[u], J = ovJ[u];
+  const int* o = off + 6 * u;
+  for (int k = threadIdx.x; k < nr; k += blockDim.x) {
+    unsigned long long key = stage_key[so + k];
+    int sub = (int)(key >> 60);
+    int i = (int)((key >> 30) & 0x3fffffffull), j = (int)(key & 0x3fffffffull);
+    int la = sub == 0 ? 0 : (sub == 1 ? 3 : 1), lb = sub == 0 ? 5 : (sub == 1 ? 2 : 4);
+    int A = (sub == 1) ? J : I, B = (sub == 1) ? I : J;
+    int a_id = lst[o[la] + i], b_id = lst[o[lb] + j];
+    if (sub < 2) {
+      int idx = ov_pt_off[u] + k;
+      out.pt[4 * idx] = A; out.pt[4 * idx + 1] = a_id; out.pt[4 * idx + 2] = B; out.pt[4 * idx + 3] = b_id;
+      out.pt_ty[idx] = stage_ty[so + k];
+      out.pt_ov[idx] = u;
+    } else {
+      int idx = ov_ee_off[u] + (k - sc[0] - sc[1]);
+      out.ee[4 * idx] = A; out.ee[4 * idx + 1] = a_id; out.ee[4 * idx + 2] = B; out.ee[4 * idx + 3] = b_id;
+      out.ee_ty[idx] = stage_ty[so + k];
+      out.ee_ov[idx] = u;
+    }
   }
 }
 
@@ -434,12 +528,13 @@ __global__ void __launch_bounds__(NT) k_narrow_scan(Geo g, Params P, float ds_f,
 __global__ void __launch_bounds__(NT) k_narrow_write(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
                                                      const int* cnt, const int* off, const int* lst, const float* vb,
                                                      const float* eb, const float* fb, const int* sub_cnt,
-                                                     const int* ov_pt_off, const int* ov_ee_off, NarrowOut out) {
+                                                     const int* ov_pt_off, const int* ov_ee_off, NarrowOut out,
+                                                     const int* stage_off) {
   __shared__ float sA[TILE * 6], sB[TILE * 6];
   __shared__ int wcnt[NT / 32];
   const int u = blockIdx.x;
   const int* sc = sub_cnt + 3 * u;
-  if (sc[0] + sc[1] + sc[2] == 0) return;
+  if (sc[0] + sc[1] + sc[2] == 0 || stage_off[u] >= 0) return;
   const int* n = cnt + 6 * u;
   const int* o = off + 6 * u;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -676,7 +771,8 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
       prof_work(K_NARROW_TOI, nov, 48.0 * g.nv);  // positions at q and q + dq
       KLAUNCH(K_NARROW_TOI, s, k_narrow_scan<2><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
-                                                                   cs.fbox.p, nullptr, cs.toi_key.p));
+                                                                   cs.fbox.p, nullptr, cs.toi_key.p, nullptr, nullptr,
+                                                                   nullptr, nullptr, 0));
     }
     if (P.ground && g.nv) {
       KLAUNCH(K_VG_TOI, s, k_vg_toi<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, cs.toi_key.p + 1));
@@ -695,9 +791,25 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     cs.blk_a_off.ensure(nov + 1);
     cs.blk_b_off.ensure(nov + 1);
     cs.sub_cnt.ensure(3 * (size_t)nov + 3);
-    KLAUNCH(K_NARROW_FLAGS, s, k_narrow_scan<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
-                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
-                                                                    cs.fbox.p, cs.sub_cnt.p, nullptr));
+    cs.stage_off.ensure(nov + 1);
+    if (cs.stage_key.cap < (1u << 16)) {
+      cs.stage_key.ensure(1u << 16);
+      cs.stage_ty.ensure(1u << 16);
+    }
+    for (int attempt = 0; attempt < 4; ++attempt) {
+      CK(cudaMemsetAsync(d_tot + 6, 0, sizeof(int), s));
+      KLAUNCH(K_NARROW_FLAGS, s, k_narrow_scan<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
+                                                                      cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
+                                                                      cs.fbox.p, cs.sub_cnt.p, nullptr, cs.stage_key.p,
+                                                                      cs.stage_ty.p, cs.stage_off.p, d_tot + 6,
+                                                                      (int)cs.stage_key.cap));
+      CK(cudaMemcpyAsync(cs.h_small + 6, d_tot + 6, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if ((size_t)cs.h_small[6] <= cs.stage_key.cap) break;
+      // staging overflowed: grow to the reported total and classify again
+      cs.stage_key.ensure((size_t)cs.h_small[6] + (cs.h_small[6] >> 2) + 1024);
+      cs.stage_ty.ensure(cs.stage_key.cap);
+    }
     KLAUNCH(K_NARROW_FLAGS, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
     scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
     scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
@@ -713,10 +825,13 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     S.ee_ty.ensure(nee + 1);
     S.ee_ov.ensure(nee + 1);
     no = NarrowOut{S.pt.p, S.pt_ov.p, S.ee.p, S.ee_ov.p, S.pt_ty.p, S.ee_ty.p};
+    KLAUNCH(K_NARROW_WRITE, s, k_narrow_copy<<<nov, 128, 0, s>>>(nov, S.ovI.p, S.ovJ.p, cs.bin_off.p, cs.lst.p,
+                                                                  cs.sub_cnt.p, cs.stage_key.p, cs.stage_ty.p,
+                                                                  cs.stage_off.p, cs.blk_a_off.p, cs.blk_b_off.p, no));
     KLAUNCH(K_NARROW_WRITE, s, k_narrow_write<<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
                                                                   cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
                                                                   cs.fbox.p, cs.sub_cnt.p, cs.blk_a_off.p,
-                                                                  cs.blk_b_off.p, no));
+                                                                  cs.blk_b_off.p, no, cs.stage_off.p));
   }
   S.npt = npt;
   S.nee = nee;
