@@ -112,6 +112,20 @@ class ABD:
         L.lib().abd_set_iter(self._h, int(v))
 
     # --- per-kernel device timing -----------------------------------------------------
+    @property
+    def n_scenes(self) -> int:
+        return L.lib().abd_get_scene_count(self._h)
+
+    def scene_stats(self) -> dict:
+        """Per-scene Newton iterations, line-search trials and PCG iterations of the last
+        step call, and each scene's cumulative Newton counter (batched mode)."""
+        ns = self.n_scenes
+        out = {k: np.zeros(ns, dtype=np.int32) for k in ("newton_iters", "ls_trials", "pcg_iters", "iter")}
+        L.check(L.lib().abd_get_scene_stats(self._h, L.iptr(out["newton_iters"]), L.iptr(out["ls_trials"]),
+                                            L.iptr(out["pcg_iters"]), L.iptr(out["iter"])), self._h,
+                "abd_get_scene_stats")
+        return out
+
     def profile(self, enable: bool = True):
         L.check(L.lib().abd_profile(self._h, int(enable)), self._h, "abd_profile")
 

@@ -53,6 +53,10 @@ struct Geo {
   const double* Ic;                     // nb
   const double* rest_box;               // nb * 6 (lo, hi), inflated by sqrt(dhat)
   const int *scene_beg, *scene_end;     // nb: body range of this body's scene
+  int ns;                               // scenes (independent sub-problems of a batch)
+  const int* bscene;                    // nb: scene of each body
+  const int *sc_beg, *sc_end;           // ns: body range of each scene
+  const double* alpha_s;                // ns or null: per-scene step for positions at q + alpha dq
   const double *q, *dq, *q0, *dqdt;     // nb * 12
   double *X, *Xq, *X0;                  // 3 * nv, structure of arrays (x | y | z)
 };
@@ -93,12 +97,13 @@ struct CullScratch {
   DBuf<int> vflag_cnt, vflag_off, sub_cnt, stage_off;
   DBuf<unsigned long long> stage_key;   // sorted accepted pairs per overlap (sub, i, j)
   DBuf<int8_t> stage_ty;
-  DBuf<unsigned long long> toi_key;     // [0] pt/ee, [1] ground
+  DBuf<unsigned long long> toi_key;     // 2 per scene: pt/ee, ground
   DBuf<int> tmp_int;
   DBuf<long long> tmp_ll;
   int* h_small = nullptr;               // pinned host scratch
   long long* h_ll = nullptr;
   unsigned long long* h_toi = nullptr;
+  int h_toi_cap = 0;
 };
 
 // ---------------- launch accounting ----------------
@@ -154,7 +159,8 @@ void scan_exclusive_ll(const long long* in, long long* out, int n, long long* d_
 
 // ---------------- culling (cull.cu) ----------------
 void launch_project(const Geo& g, int which, double alpha, cudaStream_t s);
-// vtn 1/2: builds `out`; vtn 3: returns the TOIs (pt/ee, ground) through *toi_p, *toi_g.
+// vtn 1/2: builds `out`; vtn 3: writes the per-scene TOIs (pt/ee and ground, g.ns values
+// each) to toi_p and toi_g (host arrays; either may be null).
 void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs, PairSet& out, double* toi_p,
           double* toi_g, cudaStream_t s);
 
@@ -166,24 +172,30 @@ struct NewtonBufs {
   DBuf<double> ovr;          // nov * CONTRIB
   DBuf<int> has;             // nov
   DBuf<double> D, Dinv, grad;
-  DBuf<double> x, r, z, p, qv, partial;
-  DBuf<double> red;          // small reductions
+  DBuf<double> x, r, z, p, qv;
+  DBuf<double> bpA, bpB;     // per-body partial sums of the PCG
+  DBuf<double> sc_rz, sc_bb; // per-scene CG scalars
+  DBuf<int> sc_conv, sc_iters, n_active;
+  DBuf<double> red;          // chunk partial sums of the energies
+  DBuf<int> e_off, e_chunk_cnt, e_chunk_off, e_scan_tmp;
+  DBuf<double> e_out;        // per-scene energies / dot products
   DBuf<int> status;          // [0] solver status, [1] pcg iters
   double* h_red = nullptr;   // pinned
   int* h_int = nullptr;
 };
 void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& nb, cudaStream_t s);
-// Solves H x = grad; returns iterations (negative on breakdown). dq = -x written to g.dq.
-int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& nb, double rel_tol, int max_iter, double* dq, cudaStream_t s,
-              int* status);
-// Line-search energy at the trial configuration (X must hold q + alpha dq):
-// inertia + barrier over `Snew` + lagged friction over `Slag`.
-double energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_barrier_inertia,
-              NewtonBufs& nb, cudaStream_t s);
-// dots over the 12 nb dofs: out[0] = dq.grad, out[1] = |grad|^2, out[2] = |dq|^2
-void dots(int n, const double* dq, const double* grad, NewtonBufs& nb, double* out, cudaStream_t s);
-void launch_scale(double* v, int n, double s, cudaStream_t st);
-void launch_q_update(double* q, const double* dq, int n, double alpha, cudaStream_t st);
+// Solves H x = grad per scene (scenes with sc_on[s] == 0 get x = 0); dq = -x. Returns the
+// iterations of the longest scene; scene_iters (host, ns) receives each scene's count.
+int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& nb, double rel_tol, int max_iter, const int* sc_on, double* dq,
+              cudaStream_t s, int* status, int* scene_iters);
+// Line-search energy of every scene at the trial configuration (X must hold q + alpha dq):
+// inertia + barrier over `Snew` + lagged friction over `Slag`; out (host) receives ns values.
+void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_barrier_inertia,
+            NewtonBufs& nb, cudaStream_t s, double* out);
+// Per scene over its 12 n dofs: out[3s] = dq.grad, out[3s+1] = |grad|^2, out[3s+2] = |dq|^2
+void dots(const Geo& g, const double* dq, const double* grad, NewtonBufs& nb, double* out, cudaStream_t s);
+void launch_scale_scene(const Geo& g, double* v, const double* f, cudaStream_t st);
+void launch_q_update_scene(const Geo& g, double* q, const double* dq, const double* alpha, cudaStream_t st);
 void launch_frame_end(double* q, double* q0, double* dqdt, int n, double dt, cudaStream_t st);
 void launch_copy(double* dst, const double* src, int n, cudaStream_t st);
 

@@ -37,6 +37,7 @@ __global__ void k_project(Geo g, int which, double alpha) {
   int b = g.vbody[v];
   double qq[12];
   const double* q = (which == 0) ? g.q0 + 12 * b : g.q + 12 * b;
+  if (which == 2 && g.alpha_s) alpha = g.alpha_s[g.bscene[b]];
 #pragma unroll
   for (int i = 0; i < 12; ++i) qq[i] = (which == 2) ? XA(q[i], XM(g.dq[12 * b + i], alpha)) : q[i];
   d3 x = project(qq, g.rest[3 * v], g.rest[3 * v + 1], g.rest[3 * v + 2]);
@@ -58,6 +59,7 @@ __global__ void k_body_boxes(Geo g, int vtn, double alpha, double* bbox) {
   box r{mk(g.rest_box[6 * b], g.rest_box[6 * b + 1], g.rest_box[6 * b + 2]),
         mk(g.rest_box[6 * b + 3], g.rest_box[6 * b + 4], g.rest_box[6 * b + 5])};
   double q[12], qt[12];
+  if (vtn == 2 && g.alpha_s) alpha = g.alpha_s[g.bscene[b]];
 #pragma unroll
   for (int i = 0; i < 12; ++i) {
     q[i] = g.q[12 * b + i];
@@ -485,7 +487,7 @@ __global__ void __launch_bounds__(NT) k_narrow_scan(Geo g, Params P, float ds_f,
   } else {
 #pragma unroll
     for (int q = 16; q > 0; q >>= 1) tmin = dmin(tmin, __shfl_xor_sync(0xffffffffu, tmin, q));
-    if (lane == 0 && tmin < 1.0) atomicMin(toi_key, dkey(tmin));
+    if (lane == 0 && tmin < 1.0) atomicMin(toi_key + 2 * g.bscene[ovI[u]], dkey(tmin));
   }
 }
 
@@ -651,7 +653,8 @@ __global__ void k_vg_seg(int nb, int nvg, const int* vg, int* seg) {
   seg[b] = lo;
 }
 
-// 6b. ground time of impact (collision.cpp:83-105)
+// 6b. ground time of impact (collision.cpp:83-105); toi_key points at the ground slot
+// of scene 0 (slots alternate pt/ee, ground per scene).
 __global__ void k_vg_toi(Geo g, Params P, unsigned long long* toi_key) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= g.nv) return;
@@ -659,8 +662,13 @@ __global__ void k_vg_toi(Geo g, Params P, unsigned long long* toi_key) {
   if (d2 < 0) {
     double d1 = XA(g.Xq[g.nv + v], P.ground_offset);
     double t = XD(d1, XS(d1, d2));
-    if (t < 1.0) atomicMin(toi_key, dkey(t));
+    if (t < 1.0) atomicMin(toi_key + 2 * g.bscene[g.vbody[v]], dkey(t));
   }
+}
+
+__global__ void k_fill_u64(unsigned long long* p, int n, unsigned long long v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
 }
 
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -687,14 +695,15 @@ void launch_project(const Geo& g, int which, double alpha, cudaStream_t s) {
   prof_work(K_PROJECT, g.nv, 48.0 * g.nv);  // rest read + world write per vertex
 }
 
-void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs, PairSet& out, double* toi_p,
+void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& cs, PairSet& out, double* toi_p,
           double* toi_g, cudaStream_t s) {
+  Geo g = g_in;
+  if (vtn != 2) g.alpha_s = nullptr;  // per-scene steps apply to trial positions only
   const bool traj = vtn == 3;
   const int nb = g.nb;
   if (!cs.h_small) {
     CK(cudaMallocHost(&cs.h_small, 64 * sizeof(int)));
     CK(cudaMallocHost(&cs.h_ll, 8 * sizeof(long long)));
-    CK(cudaMallocHost(&cs.h_toi, 4 * sizeof(unsigned long long)));
   }
   // 1. projection
   if (vtn == 1) launch_project(g, 1, 0.0, s);
@@ -760,13 +769,17 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
   float ds_f = float_round_up(P.d_sqrt);
   NarrowOut no{};
   if (traj) {
-    cs.toi_key.ensure(2);
-    unsigned long long one[2];
+    const int nk = 2 * g.ns;
+    cs.toi_key.ensure(nk);
+    if (cs.h_toi_cap < nk) {
+      if (cs.h_toi) CK(cudaFreeHost(cs.h_toi));
+      CK(cudaMallocHost(&cs.h_toi, nk * sizeof(unsigned long long)));
+      cs.h_toi_cap = nk;
+    }
     double o = 1.0;
     unsigned long long b;
     memcpy(&b, &o, sizeof(b));
-    one[0] = one[1] = b | 0x8000000000000000ull;
-    CK(cudaMemcpyAsync(cs.toi_key.p, one, sizeof(one), cudaMemcpyHostToDevice, s));
+    KLAUNCH(K_VG_TOI, s, k_fill_u64<<<nblk(nk, 256), 256, 0, s>>>(cs.toi_key.p, nk, b | 0x8000000000000000ull));
     if (nov > 0) {
       prof_work(K_NARROW_TOI, nov, 48.0 * g.nv);  // positions at q and q + dq
       KLAUNCH(K_NARROW_TOI, s, k_narrow_scan<2><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
@@ -777,10 +790,12 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
     if (P.ground && g.nv) {
       KLAUNCH(K_VG_TOI, s, k_vg_toi<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, cs.toi_key.p + 1));
     }
-    CK(cudaMemcpyAsync(cs.h_toi, cs.toi_key.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(cs.h_toi, cs.toi_key.p, nk * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    *toi_p = key_to_double(cs.h_toi[0]);
-    *toi_g = key_to_double(cs.h_toi[1]);
+    for (int sc = 0; sc < g.ns; ++sc) {
+      if (toi_p) toi_p[sc] = key_to_double(cs.h_toi[2 * sc]);
+      if (toi_g) toi_g[sc] = key_to_double(cs.h_toi[2 * sc + 1]);
+    }
     return;
   }
   // 5. narrow phase per overlap: counts, scan, ordered write

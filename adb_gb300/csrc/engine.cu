@@ -6,6 +6,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 #include "abd_engine.h"
@@ -86,8 +87,17 @@ struct Engine {
   int cur = 0;
   CullScratch cs;
   NewtonBufs nbufs;
-  int iter = 0, g_cnt = 0, p_cnt = 0;
   int last_cull_set = 0;
+  // scenes: independent sub-problems, each with its own Newton loop, step bound and
+  // line search (a single scene is the reference's ABD::implicit_euler)
+  int ns = 1;
+  DBuf<int> bscene, sc_beg, sc_end, sc_on;
+  DBuf<double> sc_alpha, sc_factor;
+  std::vector<int> h_sc_beg, h_sc_end;
+  std::vector<int> iter, g_cnt, p_cnt;           // per scene (iter: cumulative, model/abd.h:53)
+  std::vector<int> sc_newton, sc_ls, sc_pcg;     // per scene, over the last abd_step call
+  int* h_on = nullptr;                           // pinned staging of per-scene uploads
+  double *h_alpha = nullptr, *h_factor = nullptr;
   std::string err;
   Prof prof;
 
@@ -98,15 +108,16 @@ struct Engine {
     g.rest = rest.p; g.vbody = vbody.p; g.ev = ev.p; g.fv = fv.p;
     g.mass = mass.p; g.Ic = Ic.p; g.rest_box = rest_box.p;
     g.scene_beg = scene_beg.p; g.scene_end = scene_end.p;
+    g.ns = ns; g.bscene = bscene.p; g.sc_beg = sc_beg.p; g.sc_end = sc_end.p; g.alpha_s = nullptr;
     g.q = q.p; g.dq = dq.p; g.q0 = q0.p; g.dqdt = dqdt.p;
     g.X = X.p; g.Xq = Xq.p; g.X0 = X0.p;
     return g;
   }
 
   ~Engine() {
-    DBuf<int>* ib[] = {&v_off, &e_off, &f_off, &vbody, &ev, &fv, &scene_beg, &scene_end};
+    DBuf<int>* ib[] = {&v_off, &e_off, &f_off, &vbody, &ev, &fv, &scene_beg, &scene_end, &bscene, &sc_beg, &sc_end, &sc_on};
     for (auto* b : ib) b->release();
-    DBuf<double>* db[] = {&rest, &mass, &Ic, &rest_box, &q, &q0, &dqdt, &dq, &X, &Xq, &X0};
+    DBuf<double>* db[] = {&rest, &mass, &Ic, &rest_box, &q, &q0, &dqdt, &dq, &X, &Xq, &X0, &sc_alpha, &sc_factor};
     for (auto* b : db) b->release();
     for (auto& S : sets) {
       S.row_ptr.release(); S.col.release(); S.upidx.release(); S.ovI.release(); S.ovJ.release();
@@ -125,9 +136,15 @@ struct Engine {
     nbufs.pt_c.release(); nbufs.ee_c.release(); nbufs.pt_seg.release(); nbufs.ee_seg.release();
     nbufs.ovr.release(); nbufs.has.release(); nbufs.D.release(); nbufs.Dinv.release(); nbufs.grad.release();
     nbufs.x.release(); nbufs.r.release(); nbufs.z.release(); nbufs.p.release(); nbufs.qv.release();
-    nbufs.partial.release(); nbufs.red.release(); nbufs.status.release();
+    nbufs.bpA.release(); nbufs.bpB.release(); nbufs.sc_rz.release(); nbufs.sc_bb.release();
+    nbufs.sc_conv.release(); nbufs.sc_iters.release(); nbufs.n_active.release();
+    nbufs.e_off.release(); nbufs.e_chunk_cnt.release(); nbufs.e_chunk_off.release(); nbufs.e_scan_tmp.release();
+    nbufs.e_out.release(); nbufs.red.release(); nbufs.status.release();
     if (nbufs.h_red) cudaFreeHost(nbufs.h_red);
     if (nbufs.h_int) cudaFreeHost(nbufs.h_int);
+    if (h_on) cudaFreeHost(h_on);
+    if (h_alpha) cudaFreeHost(h_alpha);
+    if (h_factor) cudaFreeHost(h_factor);
     if (s) cudaStreamDestroy(s);
   }
 
@@ -195,18 +212,43 @@ struct Engine {
       }
     }
     // scene ranges (bodies of a scene are contiguous)
+    std::vector<int> hbs(nb);
+    std::unordered_set<int> seen;
+    h_sc_beg.clear();
+    h_sc_end.clear();
     for (int b = 0; b < nb;) {
       int e = b + 1;
       if (d->scene_id)
         while (e < nb && d->scene_id[e] == d->scene_id[b]) ++e;
       else
         e = nb;
+      if (d->scene_id && !seen.insert(d->scene_id[b]).second)
+        throw std::invalid_argument("bodies of a scene must be contiguous");
       for (int k = b; k < e; ++k) {
         sb[k] = b;
         se[k] = e;
+        hbs[k] = (int)h_sc_beg.size();
       }
+      h_sc_beg.push_back(b);
+      h_sc_end.push_back(e);
       b = e;
     }
+    ns = (int)h_sc_beg.size();
+    iter.assign(ns, 0);
+    g_cnt.assign(ns, 0);
+    p_cnt.assign(ns, 0);
+    sc_newton.assign(ns, 0);
+    sc_ls.assign(ns, 0);
+    sc_pcg.assign(ns, 0);
+    CK(cudaMallocHost(&h_on, ns * sizeof(int)));
+    CK(cudaMallocHost(&h_alpha, ns * sizeof(double)));
+    CK(cudaMallocHost(&h_factor, ns * sizeof(double)));
+    upload(bscene, hbs.data(), nb);
+    upload(sc_beg, h_sc_beg.data(), ns);
+    upload(sc_end, h_sc_end.data(), ns);
+    sc_on.ensure(ns);
+    sc_alpha.ensure(ns);
+    sc_factor.ensure(ns);
     upload(v_off, d->vert_off, nb + 1);
     upload(e_off, d->edge_off, nb + 1);
     upload(f_off, d->face_off, nb + 1);
@@ -239,6 +281,25 @@ struct Engine {
     return (20 + 96 + 96) * P_ + 200 * P_ + 2 * 1152.0 * (nb + 2.0 * S.nov) + 2 * 96.0 * nb;
   }
 
+  // Uploads of per-scene values go through pinned staging arrays; every upload is followed
+  // by a stream synchronisation before its staging array is written again.
+  void put_on(const std::vector<char>& on) {
+    for (int k = 0; k < ns; ++k) h_on[k] = on[k] ? 1 : 0;
+    CK(cudaMemcpyAsync(sc_on.p, h_on, ns * sizeof(int), cudaMemcpyHostToDevice, s));
+  }
+  void put_alpha(const std::vector<double>& a) {
+    for (int k = 0; k < ns; ++k) h_alpha[k] = a[k];
+    CK(cudaMemcpyAsync(sc_alpha.p, h_alpha, ns * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  void put_factor(const std::vector<double>& f) {
+    for (int k = 0; k < ns; ++k) h_factor[k] = f[k];
+    CK(cudaMemcpyAsync(sc_factor.p, h_factor, ns * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+
+  // One frame of every scene. Each scene follows ABD::implicit_euler on its own: Newton
+  // iterations until its own |dq| < tol (or its own counter reaches max_iter), its own
+  // CCD bound and its own Armijo line search; a scene that has finished keeps its state
+  // while the others iterate (its dq is 0). With one scene this is the reference loop.
   int step_frame(abd_frame_stats& st) {
     using clk = std::chrono::steady_clock;
     auto ms = [](clk::time_point a, clk::time_point b) {
@@ -249,12 +310,15 @@ struct Engine {
     launch_copy(q.p, q0.p, n12, s);
     CK(cudaMemsetAsync(dq.p, 0, n12 * sizeof(double), s));
     launch_project(g, 0, 0.0, s);
-    double tp, tg;
-    cull(g, P, 1, 0.0, cs, sets[cur], &tp, &tg, s);
+    cull(g, P, 1, 0.0, cs, sets[cur], nullptr, nullptr, s);
     st.bytes_moved += bytes_cull(sets[cur]);
-    bool term = false;
+    std::vector<char> act(ns, 1), ls(ns, 0), stalled(ns, 0);
+    std::vector<double> dd(3 * ns), sup_dq(ns), tp(ns, 1.0), tg(ns, 1.0), toi(ns, 1.0), fac(ns, 1.0);
+    std::vector<double> E0(ns), E1(ns), qdg(ns), gn(ns), dqn(ns), a_cull(ns, 1.0), a_fin(ns, 1.0);
+    std::vector<int> trials(ns, 0), its_s(ns, 0);
+    int n_act = ns;
     int status = ABD_OK;
-    do {
+    while (n_act > 0) {
       auto t0 = clk::now();
       PairSet& S = sets[cur];
       st.n_pt = std::max(st.n_pt, S.npt);
@@ -262,72 +326,107 @@ struct Engine {
       st.n_vg = std::max(st.n_vg, S.nvg);
       st.n_overlaps = std::max(st.n_overlaps, S.nov);
       assemble(g, P, S, nbufs, s);
-      CK(cudaStreamSynchronize(s));
+      put_on(act);
       st.bytes_moved += bytes_assemble(S);
       auto t1 = clk::now();
       int pst = 0;
-      int its = pcg_solve(g, S, nbufs, cfg.pcg_rel_tol, cfg.pcg_max_iter, dq.p, s, &pst);
+      int its = pcg_solve(g, S, nbufs, cfg.pcg_rel_tol, cfg.pcg_max_iter, sc_on.p, dq.p, s, &pst, its_s.data());
       st.pcg_iters += its;
+      for (int k = 0; k < ns; ++k) sc_pcg[k] += its_s[k];
       st.bytes_moved += its * (1152.0 * (nb + 2.0 * S.nov) + 6 * 96.0 * nb) + 1152.0 * nb;
       if (pst == ABD_ERR_NOT_SPD) return ABD_ERR_NOT_SPD;
       if (pst == ABD_ERR_PCG_NOCONV) status = ABD_ERR_PCG_NOCONV;
-      double dd[3];
-      dots(n12, dq.p, nbufs.grad.p, nbufs, dd, s);
-      double sup_dq = std::sqrt(dd[2]);
-      if (std::isnan(sup_dq)) return ABD_ERR_NAN;
+      dots(g, dq.p, nbufs.grad.p, nbufs, dd.data(), s);
+      for (int k = 0; k < ns; ++k) {
+        sup_dq[k] = std::sqrt(dd[3 * k + 2]);
+        if (act[k] && std::isnan(sup_dq[k])) return ABD_ERR_NAN;
+      }
       auto t2 = clk::now();
       // CCD step bound (abd.cpp:142-196)
-      double toi = 1.0, factor = 1.0;
+      for (int k = 0; k < ns; ++k) toi[k] = 1.0;
       if (cfg.upper_bound) {
-        cull(g, P, 3, 1.0, cs, sets[2], &tp, &tg, s);
+        cull(g, P, 3, 1.0, cs, sets[2], tp.data(), tg.data(), s);
         st.bytes_moved += 96.0 * nv + 20.0 * sets[2].nov;
-        if (cfg.ground) {
-          if (tg < 1e-6) g_cnt++;
-          else g_cnt = 0;
+        for (int k = 0; k < ns; ++k) {
+          if (!act[k]) continue;
+          if (cfg.ground) {
+            if (tg[k] < 1e-6) g_cnt[k]++;
+            else g_cnt[k] = 0;
+          }
+          if (tp[k] < 1e-6) p_cnt[k]++;
+          else p_cnt[k] = 0;
+          toi[k] = cfg.ground ? std::min(tg[k], tp[k]) : tp[k];
+          if ((cfg.ground && g_cnt[k] > 1) || p_cnt[k] > 1) return ABD_ERR_TOI_TINY;
         }
-        if (tp < 1e-6) p_cnt++;
-        else p_cnt = 0;
-        toi = cfg.ground ? std::min(tg, tp) : tp;
-        if ((cfg.ground && g_cnt > 1) || p_cnt > 1) return ABD_ERR_TOI_TINY;
       }
-      if (toi < 1.0) factor = cfg.backoff;
-      st.toi_min = std::min(st.toi_min, toi);
-      launch_scale(dq.p, n12, factor * toi, s);
+      for (int k = 0; k < ns; ++k) {
+        double factor = toi[k] < 1.0 ? cfg.backoff : 1.0;
+        fac[k] = factor * toi[k];
+        if (act[k]) st.toi_min = std::min(st.toi_min, toi[k]);
+      }
+      put_factor(fac);
+      launch_scale_scene(g, dq.p, sc_factor.p, s);
       auto t3 = clk::now();
-      // line search (line_search.cpp:39-136)
-      double alpha = 1.0;
+      // line search (line_search.cpp:39-136), all scenes' trials in one culling pass
+      for (int k = 0; k < ns; ++k) a_fin[k] = act[k] ? 1.0 : 0.0;
       if (cfg.line_search) {
         launch_project(g, 1, 0.0, s);
-        double E0 = energy(g, P, 0.0, S, S, true, nbufs, s);
-        dots(n12, dq.p, nbufs.grad.p, nbufs, dd, s);
-        double qdg = dd[0], gn = std::sqrt(dd[1]), dqn = std::sqrt(dd[2]);
+        energy(g, P, 0.0, S, S, true, nbufs, s, E0.data());
+        dots(g, dq.p, nbufs.grad.p, nbufs, dd.data(), s);
+        for (int k = 0; k < ns; ++k) {
+          qdg[k] = dd[3 * k];
+          gn[k] = std::sqrt(dd[3 * k + 1]);
+          dqn[k] = std::sqrt(dd[3 * k + 2]);
+          ls[k] = act[k];
+          stalled[k] = act[k];
+          trials[k] = 0;
+          a_cull[k] = act[k] ? 1.0 : 0.0;
+        }
         int other = 1 - cur;
-        int trials = 0;
-        bool stalled = true;
-        for (int guard = 0; guard < 2200; ++guard) {
-          cull(g, P, 2, alpha, cs, sets[other], &tp, &tg, s);
-          double E1 = energy(g, P, alpha, sets[other], S, true, nbufs, s);
-          ++trials;
+        int n_ls = n_act;
+        Geo gt = g;
+        gt.alpha_s = sc_alpha.p;
+        while (n_ls > 0) {
+          put_alpha(a_cull);
+          cull(gt, P, 2, 0.0, cs, sets[other], nullptr, nullptr, s);
+          energy(gt, P, 0.0, sets[other], S, true, nbufs, s, E1.data());
           st.bytes_moved += bytes_cull(sets[other]) + 48.0 * nv + 116.0 * (sets[other].npt + sets[other].nee);
-          bool wolfe = E1 <= E0 + cfg.c1 * alpha * qdg;
-          alpha /= 2;
-          if (!(!wolfe && gn > cfg.ls_grad_tol)) {
-            stalled = false;
-            break;
-          }
-          if (dqn * alpha * 2 < cfg.tol && cfg.clip) {
-            alpha = 0.0;
-            stalled = false;
-            break;
+          for (int k = 0; k < ns; ++k) {
+            if (!ls[k]) continue;
+            ++trials[k];
+            bool wolfe = E1[k] <= E0[k] + cfg.c1 * a_cull[k] * qdg[k];
+            double alpha = a_cull[k] / 2;
+            bool done = false;
+            if (!(!wolfe && gn[k] > cfg.ls_grad_tol)) {
+              stalled[k] = 0;
+              done = true;
+            } else if (dqn[k] * alpha * 2 < cfg.tol && cfg.clip) {
+              alpha = 0.0;
+              stalled[k] = 0;
+              done = true;
+            } else if (trials[k] >= 2200) {
+              done = true;  // stalled: keeps the last trial's step and set
+            }
+            if (done) {
+              ls[k] = 0;
+              --n_ls;
+              a_fin[k] = alpha * 2;
+            } else {
+              a_cull[k] = alpha;
+            }
           }
         }
-        st.ls_trials += trials;
-        if (stalled) status = ABD_ERR_LS_STALL;
+        for (int k = 0; k < ns; ++k) {
+          st.ls_trials += trials[k];
+          sc_ls[k] += trials[k];
+          if (stalled[k]) status = ABD_ERR_LS_STALL;
+        }
         cur = other;
-        alpha *= 2;
       }
-      st.alpha_min = std::min(st.alpha_min, alpha);
-      launch_q_update(q.p, dq.p, n12, alpha, s);
+      for (int k = 0; k < ns; ++k)
+        if (act[k]) st.alpha_min = std::min(st.alpha_min, a_fin[k]);
+      put_alpha(a_fin);
+      launch_q_update_scene(g, q.p, dq.p, sc_alpha.p, s);
       if (!cfg.line_search) launch_project(g, 1, 0.0, s);
       CK(cudaStreamSynchronize(s));
       auto t4 = clk::now();
@@ -336,9 +435,17 @@ struct Engine {
       st.t_ccd_ms += ms(t2, t3);
       st.t_ls_ms += ms(t3, t4);
       st.newton_iters++;
-      term = sup_dq < cfg.tol || ++iter >= cfg.max_iter;
-    } while (!term);
-    ++iter;
+      for (int k = 0; k < ns; ++k) {
+        if (!act[k]) continue;
+        sc_newton[k]++;
+        bool term = sup_dq[k] < cfg.tol || ++iter[k] >= cfg.max_iter;
+        if (term) {
+          act[k] = 0;
+          --n_act;
+        }
+      }
+    }
+    for (int k = 0; k < ns; ++k) ++iter[k];
     launch_frame_end(q.p, q0.p, dqdt.p, n12, P.dt, s);
     CK(cudaStreamSynchronize(s));
     last_cull_set = cur;
@@ -415,6 +522,9 @@ int abd_step(abd_handle* h, double dt, int n_frames, abd_frame_stats* stats) {
     st.toi_min = 1.0;
     st.alpha_min = 1.0;
     if (dt > 0) h->e.P.dt = dt;
+    std::fill(h->e.sc_newton.begin(), h->e.sc_newton.end(), 0);
+    std::fill(h->e.sc_ls.begin(), h->e.sc_ls.end(), 0);
+    std::fill(h->e.sc_pcg.begin(), h->e.sc_pcg.end(), 0);
     long long launches0 = h->e.prof.launches;
     cudaEvent_t ev0, ev1;
     CK(cudaEventCreate(&ev0));
@@ -475,7 +585,20 @@ int abd_get_counts(abd_handle* h, int* n_bodies, int* n_vertices, int* n_edges, 
   return ABD_OK;
 }
 
-int abd_get_iter(abd_handle* h) { return h ? h->e.iter : -1; }
+int abd_get_iter(abd_handle* h) { return h ? h->e.iter[0] : -1; }
+
+int abd_get_scene_count(abd_handle* h) { return h ? h->e.ns : -1; }
+
+int abd_get_scene_stats(abd_handle* h, int* newton_iters, int* ls_trials, int* pcg_iters, int* iter) {
+  if (!h) return ABD_ERR_INVALID;
+  for (int k = 0; k < h->e.ns; ++k) {
+    if (newton_iters) newton_iters[k] = h->e.sc_newton[k];
+    if (ls_trials) ls_trials[k] = h->e.sc_ls[k];
+    if (pcg_iters) pcg_iters[k] = h->e.sc_pcg[k];
+    if (iter) iter[k] = h->e.iter[k];
+  }
+  return ABD_OK;
+}
 
 int abd_profile(abd_handle* h, int enable) {
   if (!h) return ABD_ERR_INVALID;
@@ -510,7 +633,7 @@ int abd_kernel_work(abd_handle* h, int max_n, char* names, double* total_ms, lon
 }
 int abd_set_iter(abd_handle* h, int it) {
   if (!h) return ABD_ERR_INVALID;
-  h->e.iter = it;
+  for (auto& v : h->e.iter) v = it;
   return ABD_OK;
 }
 
@@ -522,13 +645,15 @@ int abd_cull(abd_handle* h, int vtn, const double* q, const double* dq, int* cou
     CK(cudaMemcpyAsync(e.q.p, q, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
     if (dq) CK(cudaMemcpyAsync(e.dq.p, dq, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
     else CK(cudaMemsetAsync(e.dq.p, 0, n * sizeof(double), e.s));
-    double tp = 1.0, tg = 1.0;
+    std::vector<double> tp(e.ns, 1.0), tg(e.ns, 1.0);
     abd::Geo g = e.geo();
     abd::PairSet& S = e.sets[e.cur];
-    abd::cull(g, e.P, vtn, 1.0, e.cs, vtn == 3 ? e.sets[2] : S, &tp, &tg, e.s);
+    abd::cull(g, e.P, vtn, 1.0, e.cs, vtn == 3 ? e.sets[2] : S, tp.data(), tg.data(), e.s);
     CK(cudaStreamSynchronize(e.s));
     if (vtn == 3) {
-      if (toi) *toi = e.cfg.ground ? std::min(tp, tg) : tp;
+      double t = 1.0;
+      for (int k = 0; k < e.ns; ++k) t = std::min(t, e.cfg.ground ? std::min(tp[k], tg[k]) : tp[k]);
+      if (toi) *toi = t;
       if (counts) counts[3] = e.sets[2].nov;
     } else {
       e.last_cull_set = e.cur;
@@ -571,8 +696,7 @@ static int newton_system_at(Engine& e, const double* q) {
   CK(cudaMemsetAsync(e.dq.p, 0, n * sizeof(double), e.s));
   abd::Geo g = e.geo();
   abd::launch_project(g, 0, 0.0, e.s);
-  double tp, tg;
-  abd::cull(g, e.P, 1, 0.0, e.cs, e.sets[e.cur], &tp, &tg, e.s);
+  abd::cull(g, e.P, 1, 0.0, e.cs, e.sets[e.cur], nullptr, nullptr, e.s);
   abd::assemble(g, e.P, e.sets[e.cur], e.nbufs, e.s);
   CK(cudaStreamSynchronize(e.s));
   e.last_cull_set = e.cur;
@@ -617,7 +741,9 @@ int abd_newton_dq(abd_handle* h, const double* q, double* dq, int* pcg_iters) {
     Engine& e = h->e;
     newton_system_at(e, q);
     int st = 0;
-    int its = abd::pcg_solve(e.geo(), e.sets[e.cur], e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.dq.p, e.s, &st);
+    e.put_on(std::vector<char>(e.ns, 1));
+    int its = abd::pcg_solve(e.geo(), e.sets[e.cur], e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.sc_on.p,
+                             e.dq.p, e.s, &st, nullptr);
     if (pcg_iters) *pcg_iters = its;
     CK(cudaMemcpy(dq, e.dq.p, 12 * (size_t)e.nb * sizeof(double), cudaMemcpyDeviceToHost));
     return st;

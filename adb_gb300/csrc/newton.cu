@@ -366,14 +366,31 @@ __global__ void k_block_inverse(int nb, const double* D, double* Dinv, int* stat
 // ---------------------------------------------------------------------------------
 // Block-Jacobi PCG, one cooperative launch; slots (body, row) in groups of 16 lanes so
 // the 12 rows of a body always sit in one warp.
+//
+// Every scene of a batch runs its own CG (its own alpha, beta and stopping test), so a
+// scene solved in a batch gets exactly the iterates it gets when solved alone. Dot
+// products are reduced per body (16-lane shuffle tree), then per scene over the scene's
+// bodies in a scene-relative order (thread t of a 256-thread block takes bodies
+// beg + t, beg + t + 256, ...), which does not depend on where the scene sits in the
+// batch. Every block that holds bodies of a scene computes that scene's sums itself
+// (no extra grid barrier); the block holding the scene's first body publishes the
+// scalars carried to the next iteration, in buffers alternating by iteration parity.
 struct PcgArgs {
-  int nb;
+  int nb, ns;
   const int *row_ptr, *col, *upidx, *has;
   const double *ovr, *D, *Dinv, *b;
-  double *x, *r, *z, *p, *q, *partial, *dq;
+  const int *bscene, *sc_beg, *sc_end;  // body -> scene; body range of each scene
+  const int* sc_on;                     // ns: 0 -> the scene is not solved (dq = 0)
+  double *x, *r, *z, *p, *q, *dq;
+  double *bpA, *bpB;                    // 2 nb per-body partial sums
+  double *sc_rz;                        // 2 ns (parity)
+  double *sc_bb;                        // ns
+  int *sc_conv;                         // 2 ns (parity)
+  int *sc_iters;                        // ns
+  int *n_active;                        // 2 (parity)
   double tol2;
   int maxit;
-  int* out;  // [0] status, [1] iterations
+  int* out;  // [0] status, [1] iterations (max over scenes)
 };
 
 __device__ __forceinline__ double row_spmv(const PcgArgs& a, int body, int row, const double* v) {
@@ -422,24 +439,18 @@ __device__ __forceinline__ void block_sum2(double& a, double& b, double* sh) {
   }
 }
 
-// Sums the per-block partials of one slot in a fixed order; result broadcast to the block.
-__device__ __forceinline__ void grid_sum2(const double* part, double& a, double& b, double* sh) {
-  if (threadIdx.x < 32) {
-    int lane = threadIdx.x;
-    double sa = 0, sb = 0;
-    for (int i = lane; i < (int)gridDim.x; i += 32) {
-      sa += part[2 * i];
-      sb += part[2 * i + 1];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      sa += __shfl_xor_sync(0xffffffffu, sa, o);
-      sb += __shfl_xor_sync(0xffffffffu, sb, o);
-    }
-    if (lane == 0) {
-      sh[64] = sa;
-      sh[65] = sb;
-    }
+// Block-wide sums of v[2k], v[2k+1] over bodies k in [beg, end), in the scene-relative
+// order described above; the result is broadcast to every thread of the block.
+__device__ __forceinline__ void scene_sum2(const double* v, int beg, int end, double& a, double& b, double* sh) {
+  double sa = 0.0, sb = 0.0;
+  for (int k = beg + (int)threadIdx.x; k < end; k += blockDim.x) {
+    sa += v[2 * k];
+    sb += v[2 * k + 1];
+  }
+  block_sum2(sa, sb, sh);
+  if (threadIdx.x == 0) {
+    sh[64] = sa;
+    sh[65] = sb;
   }
   __syncthreads();
   a = sh[64];
@@ -447,78 +458,135 @@ __device__ __forceinline__ void grid_sum2(const double* part, double& a, double&
   __syncthreads();
 }
 
+// Sum over the 16 lanes of a body's slot group (rows 12..15 contribute 0).
+__device__ __forceinline__ double body_sum16(double v) {
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+
 __global__ void __launch_bounds__(256) k_pcg(PcgArgs a) {
   cg::grid_group grid = cg::this_grid();
   __shared__ double sh[80];
+  __shared__ double s_val[16];   // per scene of the current body group: alpha or beta
+  __shared__ int s_flag[16];     // per scene of the current body group: converged now
   const int nslot = a.nb * 16;
   const int nthr = gridDim.x * blockDim.x;
   const int nloop = (nslot + nthr - 1) / nthr;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  double* P0 = a.partial;                       // slot 0: (rz, bb)
-  double* P1 = a.partial + 2 * gridDim.x;       // slot 1: (pq, -)
-  double* P2 = a.partial + 4 * gridDim.x;       // slot 2: (rr, rz)
-  // init: x = 0, r = b, z = M^-1 b, p = z
-  double l0 = 0, l1 = 0;
+
+  // scenes [s_lo, s_hi] of the 16-body group this block handles in loop step `it`
+  auto group = [&](int it, int& b0, int& s_lo, int& s_hi) {
+    b0 = (blockIdx.x * blockDim.x + it * nthr) >> 4;
+    if (b0 >= a.nb) {
+      s_lo = 0;
+      s_hi = -1;
+      return;
+    }
+    int b1 = b0 + 15 < a.nb ? b0 + 15 : a.nb - 1;
+    s_lo = a.bscene[b0];
+    s_hi = a.bscene[b1];
+  };
+
+  // ---- init: x = 0, r = b, z = M^-1 b, p = z (zero for scenes not solved) ----
   for (int it = 0; it < nloop; ++it) {
     int s = tid + it * nthr;
     int body = s >> 4, row = s & 15;
+    double c0 = 0.0, c1 = 0.0;
     if (s < nslot && row < 12) {
       int idx = 12 * body + row;
-      double bv = a.b[idx];
+      bool on = a.sc_on[a.bscene[body]] != 0;
+      double bv = on ? a.b[idx] : 0.0;
+      double zv = 0.0;
+      if (on) {
+        const double* Mi = a.Dinv + 144 * body + 12 * row;
+#pragma unroll
+        for (int c = 0; c < 12; ++c) zv += Mi[c] * a.b[12 * body + c];
+      }
       a.x[idx] = 0.0;
       a.r[idx] = bv;
-      const double* Mi = a.Dinv + 144 * body + 12 * row;
-      double zv = 0;
-#pragma unroll
-      for (int c = 0; c < 12; ++c) zv += Mi[c] * a.b[12 * body + c];
       a.z[idx] = zv;
       a.p[idx] = zv;
-      l0 += bv * zv;
-      l1 += bv * bv;
+      c0 = bv * zv;
+      c1 = bv * bv;
+    }
+    c0 = body_sum16(c0);
+    c1 = body_sum16(c1);
+    if (s < nslot && row == 0) {
+      a.bpA[2 * body] = c0;
+      a.bpA[2 * body + 1] = c1;
     }
   }
-  block_sum2(l0, l1, sh);
-  if (threadIdx.x == 0) {
-    P0[2 * blockIdx.x] = l0;
-    P0[2 * blockIdx.x + 1] = l1;
+  grid.sync();
+  for (int it = 0; it < nloop; ++it) {
+    int b0, s_lo, s_hi;
+    group(it, b0, s_lo, s_hi);
+    for (int sc = s_lo; sc <= s_hi; ++sc) {
+      if (a.sc_beg[sc] < b0) continue;  // published by the group holding the scene's first body
+      double rz, bb;
+      scene_sum2(a.bpA, a.sc_beg[sc], a.sc_end[sc], rz, bb, sh);
+      if (threadIdx.x == 0) {
+        bool conv = !a.sc_on[sc] || bb == 0.0;
+        a.sc_rz[sc] = rz;
+        a.sc_bb[sc] = bb;
+        a.sc_conv[sc] = conv ? 1 : 0;
+        a.sc_iters[sc] = 0;
+        if (!conv) atomicAdd(&a.n_active[0], 1);
+      }
+    }
   }
   grid.sync();
-  double rz, bb;
-  grid_sum2(P0, rz, bb, sh);
-  int iters = 0;
-  bool conv = (bb == 0.0);
-  for (int k = 0; k < a.maxit && !conv; ++k) {
-    double lp = 0, dummy = 0;
+  int nact = ld_volatile(&a.n_active[0]);
+  int k = 0;
+  for (; k < a.maxit && nact > 0; ++k) {
+    const int par = k & 1, nxt = par ^ 1;
+    const double* rz_cur = a.sc_rz + par * a.ns;
+    double* rz_nxt = a.sc_rz + nxt * a.ns;
+    const int* conv_cur = a.sc_conv + par * a.ns;
+    int* conv_nxt = a.sc_conv + nxt * a.ns;
+    if (tid == 0) a.n_active[nxt] = 0;
+    // ---- A: q = H p, per-body p.q ----
     for (int it = 0; it < nloop; ++it) {
       int s = tid + it * nthr;
       int body = s >> 4, row = s & 15;
-      if (s < nslot && row < 12) {
+      double c0 = 0.0;
+      if (s < nslot && row < 12 && !conv_cur[a.bscene[body]]) {
         int idx = 12 * body + row;
         double qv = row_spmv(a, body, row, a.p);
         a.q[idx] = qv;
-        lp += a.p[idx] * qv;
+        c0 = a.p[idx] * qv;
+      }
+      c0 = body_sum16(c0);
+      if (s < nslot && row == 0) {
+        a.bpA[2 * body] = c0;
+        a.bpA[2 * body + 1] = 0.0;
       }
     }
-    block_sum2(lp, dummy, sh);
-    if (threadIdx.x == 0) {
-      P1[2 * blockIdx.x] = lp;
-      P1[2 * blockIdx.x + 1] = 0.0;
-    }
     grid.sync();
-    double pq;
-    grid_sum2(P1, pq, dummy, sh);
-    double alpha = rz / pq;
-    double lrr = 0, lrz = 0;
+    // ---- B: alpha per scene; x += alpha p, r -= alpha q, z = M^-1 r; per-body r.r, r.z ----
     for (int it = 0; it < nloop; ++it) {
+      int b0, s_lo, s_hi;
+      group(it, b0, s_lo, s_hi);
+      for (int sc = s_lo; sc <= s_hi; ++sc) {
+        if (conv_cur[sc]) continue;
+        double pq, dummy;
+        scene_sum2(a.bpA, a.sc_beg[sc], a.sc_end[sc], pq, dummy, sh);
+        if (threadIdx.x == 0) s_val[sc - s_lo] = rz_cur[sc] / pq;
+      }
+      __syncthreads();
       int s = tid + it * nthr;
       int body = s >> 4, row = s & 15;
-      bool act = s < nslot && row < 12;
+      bool act = s < nslot && row < 12 && !conv_cur[a.bscene[body]];
       int idx = 12 * body + row;
       if (act) {
+        double alpha = s_val[a.bscene[body] - s_lo];
         a.x[idx] += alpha * a.p[idx];
         a.r[idx] -= alpha * a.q[idx];
       }
       __syncwarp();
+      double c0 = 0.0, c1 = 0.0;
       if (act) {
         const double* Mi = a.Dinv + 144 * body + 12 * row;
         double zv = 0;
@@ -526,34 +594,56 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs a) {
         for (int c = 0; c < 12; ++c) zv += Mi[c] * a.r[12 * body + c];
         a.z[idx] = zv;
         double rv = a.r[idx];
-        lrr += rv * rv;
-        lrz += rv * zv;
+        c0 = rv * rv;
+        c1 = rv * zv;
       }
-    }
-    block_sum2(lrr, lrz, sh);
-    if (threadIdx.x == 0) {
-      P2[2 * blockIdx.x] = lrr;
-      P2[2 * blockIdx.x + 1] = lrz;
+      c0 = body_sum16(c0);
+      c1 = body_sum16(c1);
+      if (s < nslot && row == 0) {
+        a.bpB[2 * body] = c0;
+        a.bpB[2 * body + 1] = c1;
+      }
+      __syncthreads();
     }
     grid.sync();
-    double rr, rzn;
-    grid_sum2(P2, rr, rzn, sh);
-    iters = k + 1;
-    if (!(rr > a.tol2 * bb)) {
-      conv = true;
-      break;
-    }
-    double beta = rzn / rz;
-    rz = rzn;
+    // ---- C: stopping test and beta per scene; p = z + beta p ----
     for (int it = 0; it < nloop; ++it) {
+      int b0, s_lo, s_hi;
+      group(it, b0, s_lo, s_hi);
+      for (int sc = s_lo; sc <= s_hi; ++sc) {
+        bool owner = a.sc_beg[sc] >= b0;
+        if (conv_cur[sc]) {
+          if (owner && threadIdx.x == 0) conv_nxt[sc] = 1;
+          continue;
+        }
+        double rr, rzn;
+        scene_sum2(a.bpB, a.sc_beg[sc], a.sc_end[sc], rr, rzn, sh);
+        if (threadIdx.x == 0) {
+          bool conv = !(rr > a.tol2 * a.sc_bb[sc]);
+          s_val[sc - s_lo] = rzn / rz_cur[sc];
+          s_flag[sc - s_lo] = conv ? 1 : 0;
+          if (owner) {
+            rz_nxt[sc] = rzn;
+            conv_nxt[sc] = conv ? 1 : 0;
+            if (conv) a.sc_iters[sc] = k + 1;
+            else atomicAdd(&a.n_active[nxt], 1);
+          }
+        }
+      }
+      __syncthreads();
       int s = tid + it * nthr;
       int body = s >> 4, row = s & 15;
       if (s < nslot && row < 12) {
-        int idx = 12 * body + row;
-        a.p[idx] = a.z[idx] + beta * a.p[idx];
+        int sc = a.bscene[body];
+        if (!conv_cur[sc] && !s_flag[sc - s_lo]) {
+          int idx = 12 * body + row;
+          a.p[idx] = a.z[idx] + s_val[sc - s_lo] * a.p[idx];
+        }
       }
+      __syncthreads();
     }
     grid.sync();
+    nact = ld_volatile(&a.n_active[nxt]);
   }
   // dq = -x
   for (int it = 0; it < nloop; ++it) {
@@ -562,20 +652,34 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs a) {
     if (s < nslot && row < 12) a.dq[12 * body + row] = -a.x[12 * body + row];
   }
   if (tid == 0) {
-    a.out[1] = iters;
-    if (!conv) a.out[0] = ABD_ERR_PCG_NOCONV;
+    a.out[1] = k;
+    if (nact > 0) a.out[0] = ABD_ERR_PCG_NOCONV;
   }
+  // scenes still running at the iteration cap
+  if (nact > 0)
+    for (int sc = tid; sc < a.ns; sc += nthr)
+      if (!a.sc_conv[(k & 1) * a.ns + sc]) a.sc_iters[sc] = k;
 }
 
 // ---------------------------------------------------------------------------------
-// Line-search energies over a virtual index range; per-CTA partials, fixed-order sum.
+// Line-search energies, one total per scene. A scene's terms form one virtual index
+// range (its bodies, PT, EE and VG pairs of the trial set, then the PT, EE and VG pairs
+// of the lagged set); the range is cut into chunks of ECHUNK terms counted from the
+// scene's own start, each chunk is summed by one block in a fixed order, and the chunk
+// sums of a scene are added in chunk order. The total of a scene therefore does not
+// depend on where the scene sits in a batch.
+constexpr int ECHUNK = 1024;
+enum { SEG_PT, SEG_EE, SEG_VG, SEG_LPT, SEG_LEE, SEG_LVG, NSEG };
+
 struct EnergyArgs {
-  int nb, npt, nee, nvg, lpt, lee, lvg;
-  double alpha;
+  int nb, ns, npt, nee, nvg, lpt, lee, lvg;
+  double alpha;  // used when the geometry carries no per-scene step
   int with_bi;
   const int *pt, *ee, *vg, *lpt_t, *lee_t, *lvg_t;
   const double *lpt_lag, *lee_lag, *lvg_lam;
-  double* partial;
+  const int* off;        // NSEG * (ns + 1): first element of each scene in each list
+  const int* chunk_off;  // ns + 1
+  double* partial;       // one per chunk
 };
 
 __device__ double inertia_energy(const Geo& g, const Params& P, int b, double alpha) {
@@ -613,149 +717,195 @@ __device__ __forceinline__ void pair_vids(const Geo& g, int kind, const int* tup
   }
 }
 
+// One term: seg -1 = body (inertia + orthogonality), else an index into the list `seg`.
+__device__ double energy_term(const Geo& g, const Params& P, const EnergyArgs& a, int seg, int i) {
+  BarrierP bp{P.dhat, P.kappa};
+  if (seg < 0) {
+    double alpha = g.alpha_s ? g.alpha_s[g.bscene[i]] : a.alpha;
+    return inertia_energy(g, P, i, alpha);
+  }
+  if (seg == SEG_PT) {
+    if (!P.pt) return 0.0;
+    int vid[4];
+    pair_vids(g, 0, a.pt, i, vid);
+    d3 X0 = ldX(g.X, g.nv, vid[0]), X1 = ldX(g.X, g.nv, vid[1]), X2 = ldX(g.X, g.nv, vid[2]),
+       X3 = ldX(g.X, g.nv, vid[3]);
+    int ty = pt_type(X0, X1, X2, X3);
+    return barrier_b(pt_dist(X0, X1, X2, X3, ty), bp);
+  }
+  if (seg == SEG_EE) {
+    if (!P.ee) return 0.0;
+    int vid[4];
+    pair_vids(g, 1, a.ee, i, vid);
+    d3 X0 = ldX(g.X, g.nv, vid[0]), X1 = ldX(g.X, g.nv, vid[1]), X2 = ldX(g.X, g.nv, vid[2]),
+       X3 = ldX(g.X, g.nv, vid[3]);
+    d3 u = fsub(X1, X0), v = fsub(X3, X2);
+    double eps_x = fdot(fsub(X0, X1), fsub(X0, X1)) * fdot(fsub(X2, X3), fsub(X2, X3)) * P.eps_x;
+    d3 cr = fcross(u, v);
+    double x = fdot(cr, cr);
+    double m = 1.0;
+    if (x < eps_x) {
+      double xe = x / eps_x;
+      m = (-xe + 2.0) * xe;
+    }
+    int ty = ee_type(X0, X1, X2, X3);
+    return barrier_b(ee_dist(X0, X1, X2, X3, ty), bp) * m;
+  }
+  if (seg == SEG_VG) {
+    if (!P.ground) return 0.0;
+    int b = a.vg[2 * i], v = g.v_off[b] + a.vg[2 * i + 1];
+    double d = XA(g.X[g.nv + v], P.ground_offset);
+    d = XM(d, d);
+    return d < P.dhat ? barrier_b(d, bp) : 0.0;
+  }
+  if (seg == SEG_LPT || seg == SEG_LEE) {
+    int kind = seg == SEG_LEE ? 1 : 0;
+    int n = kind ? a.lee : a.lpt;
+    bool on = kind ? (P.ee && P.ee_fric) : (P.pt && P.pt_fric);
+    if (!on) return 0.0;
+    const double* L = kind ? a.lee_lag : a.lpt_lag;
+    int vid[4];
+    pair_vids(g, kind, kind ? a.lee_t : a.lpt_t, i, vid);
+    d3 c0 = fd3(L[0 * n + i], L[1 * n + i], L[2 * n + i]), c1 = fd3(L[3 * n + i], L[4 * n + i], L[5 * n + i]);
+    double u0 = 0, u1 = 0;
+    for (int k = 0; k < 4; ++k) {
+      d3 du = fsub(ldX(g.X, g.nv, vid[k]), ldX(g.X0, g.nv, vid[k]));
+      double gm = L[(6 + k) * n + i];
+      u0 += gm * fdot(c0, du);
+      u1 += gm * fdot(c1, du);
+    }
+    return P.mu * L[10 * n + i] * f0_SF(sqrt(u0 * u0 + u1 * u1), P.epsv);
+  }
+  // SEG_LVG
+  if (!(P.ground && P.vg_fric)) return 0.0;
+  int b = a.lvg_t[2 * i], v = g.v_off[b] + a.lvg_t[2 * i + 1];
+  double dx = g.X[v] - g.X0[v], dz = g.X[2 * g.nv + v] - g.X0[2 * g.nv + v];
+  return P.mu * a.lvg_lam[i] * f0_SF(sqrt(dx * dx + dz * dz), P.epsv);
+}
+
+// First element of list `tup` (stride ints per element, body id first) whose body lies in
+// scene >= s; the lists are ordered by scene.
+__device__ __forceinline__ int scene_lower_bound(const int* bscene, const int* tup, int stride, int n, int s) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (bscene[tup[stride * mid]] < s) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Per-scene list offsets and chunk counts (thread per scene, plus one for the ends).
+__global__ void k_scene_offsets(Geo g, EnergyArgs a, int* off, int* chunk_cnt) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > a.ns) return;
+  const int* lists[NSEG] = {a.pt, a.ee, a.vg, a.lpt_t, a.lee_t, a.lvg_t};
+  const int stride[NSEG] = {4, 4, 2, 4, 4, 2};
+  const int n[NSEG] = {a.npt, a.nee, a.nvg, a.lpt, a.lee, a.lvg};
+  long long total = 0;
+  for (int k = 0; k < NSEG; ++k) {
+    int lo = (s == a.ns) ? n[k] : scene_lower_bound(g.bscene, lists[k], stride[k], n[k], s);
+    off[k * (a.ns + 1) + s] = lo;
+    if (s < a.ns) {
+      if (k < SEG_LPT && !a.with_bi) continue;
+      int hi = scene_lower_bound(g.bscene, lists[k], stride[k], n[k], s + 1);
+      total += hi - lo;
+    }
+  }
+  if (s < a.ns) {
+    if (a.with_bi) total += g.sc_end[s] - g.sc_beg[s];
+    long long c = (total + ECHUNK - 1) / ECHUNK;
+    chunk_cnt[s] = c > 0 ? (int)c : 1;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_energy(Geo g, Params P, EnergyArgs a) {
   __shared__ double sh[80];
-  long long total = (long long)(a.with_bi ? a.nb + a.npt + a.nee + a.nvg : 0) + a.lpt + a.lee + a.lvg;
-  double acc = 0.0;
-  BarrierP bp{P.dhat, P.kappa};
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
-    long long i = t;
-    if (a.with_bi) {
-      if (i < a.nb) { acc += inertia_energy(g, P, (int)i, a.alpha); continue; }
-      i -= a.nb;
-      if (i < a.npt) {
-        if (P.pt) {
-          int vid[4];
-          pair_vids(g, 0, a.pt, (int)i, vid);
-          d3 X0 = ldX(g.X, g.nv, vid[0]), X1 = ldX(g.X, g.nv, vid[1]), X2 = ldX(g.X, g.nv, vid[2]),
-             X3 = ldX(g.X, g.nv, vid[3]);
-          int ty = pt_type(X0, X1, X2, X3);
-          acc += barrier_b(pt_dist(X0, X1, X2, X3, ty), bp);
-        }
-        continue;
-      }
-      i -= a.npt;
-      if (i < a.nee) {
-        if (P.ee) {
-          int vid[4];
-          pair_vids(g, 1, a.ee, (int)i, vid);
-          d3 X0 = ldX(g.X, g.nv, vid[0]), X1 = ldX(g.X, g.nv, vid[1]), X2 = ldX(g.X, g.nv, vid[2]),
-             X3 = ldX(g.X, g.nv, vid[3]);
-          d3 u = fsub(X1, X0), v = fsub(X3, X2);
-          double eps_x = fdot(fsub(X0, X1), fsub(X0, X1)) * fdot(fsub(X2, X3), fsub(X2, X3)) * P.eps_x;
-          d3 cr = fcross(u, v);
-          double x = fdot(cr, cr);
-          double m = 1.0;
-          if (x < eps_x) {
-            double xe = x / eps_x;
-            m = (-xe + 2.0) * xe;
-          }
-          int ty = ee_type(X0, X1, X2, X3);
-          acc += barrier_b(ee_dist(X0, X1, X2, X3, ty), bp) * m;
-        }
-        continue;
-      }
-      i -= a.nee;
-      if (i < a.nvg) {
-        if (P.ground) {
-          int b = a.vg[2 * i], v = g.v_off[b] + a.vg[2 * i + 1];
-          double d = XA(g.X[g.nv + v], P.ground_offset);
-          d = XM(d, d);
-          if (d < P.dhat) acc += barrier_b(d, bp);
-        }
-        continue;
-      }
-      i -= a.nvg;
+  const int nchunk = a.chunk_off[a.ns];
+  for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
+    // scene of chunk c: last s with chunk_off[s] <= c
+    int lo = 0, hi = a.ns - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (a.chunk_off[mid] <= c) lo = mid;
+      else hi = mid - 1;
     }
-    // lagged friction
-    if (i < a.lpt || (i >= a.lpt && i < a.lpt + a.lee)) {
-      int kind = (i < a.lpt) ? 0 : 1;
-      int n = kind ? a.lee : a.lpt;
-      int p = (int)(kind ? i - a.lpt : i);
-      bool on = kind ? (P.ee && P.ee_fric) : (P.pt && P.pt_fric);
-      if (!on) continue;
-      const double* L = kind ? a.lee_lag : a.lpt_lag;
-      int vid[4];
-      pair_vids(g, kind, kind ? a.lee_t : a.lpt_t, p, vid);
-      d3 c0 = fd3(L[0 * n + p], L[1 * n + p], L[2 * n + p]), c1 = fd3(L[3 * n + p], L[4 * n + p], L[5 * n + p]);
-      double u0 = 0, u1 = 0;
-      for (int k = 0; k < 4; ++k) {
-        d3 du = fsub(ldX(g.X, g.nv, vid[k]), ldX(g.X0, g.nv, vid[k]));
-        double gm = L[(6 + k) * n + p];
-        u0 += gm * fdot(c0, du);
-        u1 += gm * fdot(c1, du);
+    const int s = lo;
+    const int S1 = a.ns + 1;
+    int len[1 + NSEG], beg[1 + NSEG];
+    len[0] = a.with_bi ? g.sc_end[s] - g.sc_beg[s] : 0;
+    beg[0] = g.sc_beg[s];
+    for (int k = 0; k < NSEG; ++k) {
+      beg[k + 1] = a.off[k * S1 + s];
+      len[k + 1] = (k < SEG_LPT && !a.with_bi) ? 0 : a.off[k * S1 + s + 1] - beg[k + 1];
+    }
+    long long total = 0;
+    for (int k = 0; k <= NSEG; ++k) total += len[k];
+    long long e0 = (long long)(c - a.chunk_off[s]) * ECHUNK;
+    long long e1 = e0 + ECHUNK < total ? e0 + ECHUNK : total;
+    double acc = 0.0;
+    for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      long long i = e;
+      int k = 0;
+      while (i >= len[k]) {
+        i -= len[k];
+        ++k;
       }
-      acc += P.mu * L[10 * n + p] * f0_SF(sqrt(u0 * u0 + u1 * u1), P.epsv);
-      continue;
+      acc += energy_term(g, P, a, k - 1, beg[k] + (int)i);
     }
-    i -= a.lpt + a.lee;
-    if (i < a.lvg) {
-      if (!(P.ground && P.vg_fric)) continue;
-      int b = a.lvg_t[2 * i], v = g.v_off[b] + a.lvg_t[2 * i + 1];
-      double dx = g.X[v] - g.X0[v], dz = g.X[2 * g.nv + v] - g.X0[2 * g.nv + v];
-      acc += P.mu * a.lvg_lam[i] * f0_SF(sqrt(dx * dx + dz * dz), P.epsv);
-    }
-  }
-  double dummy = 0;
-  block_sum2(acc, dummy, sh);
-  if (threadIdx.x == 0) a.partial[blockIdx.x] = acc;
-}
-
-__global__ void k_final_sum(const double* part, int n, double* out) {
-  __shared__ double sh[32];
-  double s = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
-    *out = t;
+    double dummy = 0;
+    block_sum2(acc, dummy, sh);
+    if (threadIdx.x == 0) a.partial[c] = acc;
+    __syncthreads();
   }
 }
 
-__global__ void k_dots(int n, const double* a, const double* b, double* part) {
+__global__ void k_scene_energy(int ns, const int* chunk_off, const double* part, double* out) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  double t = 0.0;
+  for (int c = chunk_off[s]; c < chunk_off[s + 1]; ++c) t += part[c];
+  out[s] = t;
+}
+
+// Per scene: dq.grad, |grad|^2, |dq|^2 (one block per scene; thread t takes the scene's
+// bodies t, t + 256, ..., each body's 12 entries in order).
+__global__ void __launch_bounds__(256) k_scene_dots(const int* sc_beg, const int* sc_end, const double* a,
+                                                   const double* b, double* out) {
   __shared__ double sh[80];
+  int s = blockIdx.x;
   double s0 = 0, s1 = 0, s2 = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    s0 += a[i] * b[i];
-    s1 += b[i] * b[i];
-    s2 += a[i] * a[i];
+  for (int k = sc_beg[s] + (int)threadIdx.x; k < sc_end[s]; k += blockDim.x) {
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (int i = 12 * k; i < 12 * k + 12; ++i) {
+      t0 += a[i] * b[i];
+      t1 += b[i] * b[i];
+      t2 += a[i] * a[i];
+    }
+    s0 += t0;
+    s1 += t1;
+    s2 += t2;
   }
-  double t = s2;
   block_sum2(s0, s1, sh);
   __syncthreads();
   double d = 0;
-  block_sum2(t, d, sh);
+  block_sum2(s2, d, sh);
   if (threadIdx.x == 0) {
-    part[3 * blockIdx.x] = s0;
-    part[3 * blockIdx.x + 1] = s1;
-    part[3 * blockIdx.x + 2] = t;
-  }
-}
-__global__ void k_dots_final(const double* part, int nblocks, double* out) {
-  if (threadIdx.x == 0) {
-    double a = 0, b = 0, c = 0;
-    for (int i = 0; i < nblocks; ++i) {
-      a += part[3 * i];
-      b += part[3 * i + 1];
-      c += part[3 * i + 2];
-    }
-    out[0] = a;
-    out[1] = b;
-    out[2] = c;
+    out[3 * s] = s0;
+    out[3 * s + 1] = s1;
+    out[3 * s + 2] = s2;
   }
 }
 
-__global__ void k_scale(double* v, int n, double s) {
+// v *= f[scene of body]
+__global__ void k_scale_scene(double* v, int n, const int* bscene, const double* f) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) v[i] = XM(v[i], s);
+  if (i < n) v[i] = XM(v[i], f[bscene[i / 12]]);
 }
-__global__ void k_q_update(double* q, const double* dq, int n, double alpha) {
+// q += alpha[scene of body] dq
+__global__ void k_q_update_scene(double* q, const double* dq, int n, const int* bscene, const double* alpha) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) q[i] = XA(q[i], XM(dq[i], alpha));
+  if (i < n) q[i] = XA(q[i], XM(dq[i], alpha[bscene[i / 12]]));
 }
 __global__ void k_frame_end(double* q, double* q0, double* dqdt, int n, double dt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -804,9 +954,9 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
                                    S.vg_lam.p, B.D.p, B.grad.p));
 }
 
-int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_iter, double* dq, cudaStream_t s,
-              int* status) {
-  int nb = g.nb;
+int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_iter, const int* sc_on, double* dq,
+              cudaStream_t s, int* status, int* scene_iters) {
+  int nb = g.nb, ns = g.ns;
   B.status.ensure(4);
   if (!B.h_int) CK(cudaMallocHost(&B.h_int, 16 * sizeof(int)));
   CK(cudaMemsetAsync(B.status.p, 0, 4 * sizeof(int), s));
@@ -816,6 +966,14 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   B.z.ensure(12 * (size_t)nb);
   B.p.ensure(12 * (size_t)nb);
   B.qv.ensure(12 * (size_t)nb);
+  B.bpA.ensure(2 * (size_t)nb);
+  B.bpB.ensure(2 * (size_t)nb);
+  B.sc_rz.ensure(2 * (size_t)ns);
+  B.sc_bb.ensure(ns);
+  B.sc_conv.ensure(2 * (size_t)ns);
+  B.sc_iters.ensure(ns);
+  B.n_active.ensure(2);
+  CK(cudaMemsetAsync(B.n_active.p, 0, 2 * sizeof(int), s));
   static int max_blocks = 0;
   if (!max_blocks) {
     int dev, sms, per;
@@ -827,9 +985,9 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   int want = nblk((long long)nb * 16, 256);
   int grid = want < max_blocks ? want : max_blocks;
   if (grid < 1) grid = 1;
-  B.partial.ensure(6 * (size_t)grid + 8);
   PcgArgs a;
   a.nb = nb;
+  a.ns = ns;
   a.row_ptr = S.row_ptr.p;
   a.col = S.col.p;
   a.upidx = S.upidx.p;
@@ -838,19 +996,30 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   a.D = B.D.p;
   a.Dinv = B.Dinv.p;
   a.b = B.grad.p;
+  a.bscene = g.bscene;
+  a.sc_beg = g.sc_beg;
+  a.sc_end = g.sc_end;
+  a.sc_on = sc_on;
   a.x = B.x.p;
   a.r = B.r.p;
   a.z = B.z.p;
   a.p = B.p.p;
   a.q = B.qv.p;
-  a.partial = B.partial.p;
   a.dq = dq;
+  a.bpA = B.bpA.p;
+  a.bpB = B.bpB.p;
+  a.sc_rz = B.sc_rz.p;
+  a.sc_bb = B.sc_bb.p;
+  a.sc_conv = B.sc_conv.p;
+  a.sc_iters = B.sc_iters.p;
+  a.n_active = B.n_active.p;
   a.tol2 = rel_tol * rel_tol;
   a.maxit = max_iter;
   a.out = B.status.p;
   void* args[] = {&a};
   KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel((void*)k_pcg, dim3(grid), dim3(256), args, 0, s)));
   CK(cudaMemcpyAsync(B.h_int, B.status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (scene_iters) CK(cudaMemcpyAsync(scene_iters, B.sc_iters.p, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   *status = B.h_int[0];
   // per iteration: the block matrix once (1152 B per block) and ~6 vector streams
@@ -858,10 +1027,11 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   return B.h_int[1];
 }
 
-double energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_bi,
-              NewtonBufs& B, cudaStream_t s) {
+void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_bi, NewtonBufs& B,
+            cudaStream_t s, double* out) {
   EnergyArgs a;
   a.nb = g.nb;
+  a.ns = g.ns;
   a.npt = Snew.npt;
   a.nee = Snew.nee;
   a.nvg = Snew.nvg;
@@ -879,39 +1049,45 @@ double energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSe
   a.lpt_lag = Slag.pt_lag.p;
   a.lee_lag = Slag.ee_lag.p;
   a.lvg_lam = Slag.vg_lam.p;
-  const int G = 512;
-  B.red.ensure(G + 8);
+  const int ns = g.ns;
+  B.e_off.ensure((size_t)NSEG * (ns + 1));
+  B.e_chunk_cnt.ensure(ns + 1);
+  B.e_chunk_off.ensure(ns + 1);
+  B.e_out.ensure(ns);
+  a.off = B.e_off.p;
+  a.chunk_off = B.e_chunk_off.p;
+  KLAUNCH(K_ENERGY, s, k_scene_offsets<<<nblk(ns + 1, 128), 128, 0, s>>>(g, a, B.e_off.p, B.e_chunk_cnt.p));
+  scan_exclusive_int(B.e_chunk_cnt.p, B.e_chunk_off.p, ns, B.e_chunk_off.p + ns, s, B.e_scan_tmp);
+  // chunk count bound: every scene has at least one chunk, plus one per ECHUNK terms
+  long long terms = (long long)(with_bi ? g.nb + a.npt + a.nee + a.nvg : 0) + a.lpt + a.lee + a.lvg;
+  size_t max_chunks = (size_t)ns + (size_t)(terms / ECHUNK) + 1;
+  B.red.ensure(max_chunks + 8);
   a.partial = B.red.p;
-  if (!B.h_red) CK(cudaMallocHost(&B.h_red, 16 * sizeof(double)));
+  const int G = 608;
   prof_work(K_ENERGY, (double)a.npt + a.nee + a.lpt + a.lee,
             136.0 * ((double)a.npt + a.nee + a.lpt + a.lee) + 96.0 * g.nb);
   KLAUNCH(K_ENERGY, s, k_energy<<<G, 256, 0, s>>>(g, P, a));
-  KLAUNCH(K_ENERGY, s, k_final_sum<<<1, 256, 0, s>>>(B.red.p, G, B.red.p + G));
-  CK(cudaMemcpyAsync(B.h_red, B.red.p + G, sizeof(double), cudaMemcpyDeviceToHost, s));
+  KLAUNCH(K_ENERGY, s, k_scene_energy<<<nblk(ns, 128), 128, 0, s>>>(ns, B.e_chunk_off.p, B.red.p, B.e_out.p));
+  CK(cudaMemcpyAsync(out, B.e_out.p, ns * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  return B.h_red[0];
 }
 
-void dots(int n, const double* dq, const double* grad, NewtonBufs& B, double* out, cudaStream_t s) {
-  const int G = 64;
-  B.red.ensure(3 * G + 8);
-  if (!B.h_red) CK(cudaMallocHost(&B.h_red, 16 * sizeof(double)));
-  KLAUNCH(K_DOTS, s, k_dots<<<G, 256, 0, s>>>(n, dq, grad, B.red.p));
-  KLAUNCH(K_DOTS, s, k_dots_final<<<1, 32, 0, s>>>(B.red.p, G, B.red.p + 3 * G));
-  CK(cudaMemcpyAsync(B.h_red, B.red.p + 3 * G, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+void dots(const Geo& g, const double* dq, const double* grad, NewtonBufs& B, double* out, cudaStream_t s) {
+  B.e_out.ensure(3 * (size_t)g.ns);
+  KLAUNCH(K_DOTS, s, k_scene_dots<<<g.ns, 256, 0, s>>>(g.sc_beg, g.sc_end, dq, grad, B.e_out.p));
+  CK(cudaMemcpyAsync(out, B.e_out.p, 3 * (size_t)g.ns * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  out[0] = B.h_red[0];
-  out[1] = B.h_red[1];
-  out[2] = B.h_red[2];
 }
 
-void launch_scale(double* v, int n, double sc, cudaStream_t st) {
+void launch_scale_scene(const Geo& g, double* v, const double* f, cudaStream_t st) {
+  int n = 12 * g.nb;
   if (n <= 0) return;
-  KLAUNCH(K_VEC, st, k_scale<<<nblk(n, 256), 256, 0, st>>>(v, n, sc));
+  KLAUNCH(K_VEC, st, k_scale_scene<<<nblk(n, 256), 256, 0, st>>>(v, n, g.bscene, f));
 }
-void launch_q_update(double* q, const double* dq, int n, double alpha, cudaStream_t st) {
+void launch_q_update_scene(const Geo& g, double* q, const double* dq, const double* alpha, cudaStream_t st) {
+  int n = 12 * g.nb;
   if (n <= 0) return;
-  KLAUNCH(K_VEC, st, k_q_update<<<nblk(n, 256), 256, 0, st>>>(q, dq, n, alpha));
+  KLAUNCH(K_VEC, st, k_q_update_scene<<<nblk(n, 256), 256, 0, st>>>(q, dq, n, g.bscene, alpha));
 }
 void launch_frame_end(double* q, double* q0, double* dqdt, int n, double dt, cudaStream_t st) {
   if (n <= 0) return;

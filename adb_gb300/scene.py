@@ -298,6 +298,23 @@ class Scene:
                                                      np.array(getattr(self, f.name)))
                                             for f in dataclasses.fields(self)})
 
+    def body_range(self, b0: int, b1: int) -> "Scene":
+        """Bodies [b0, b1) as a scene of their own (scene ids dropped)."""
+        vo, eo, fo = self.vert_off, self.edge_off, self.face_off
+        return Scene(q0=np.array(self.q0[b0:b1]), dqdt=np.array(self.dqdt[b0:b1]), mass=np.array(self.mass[b0:b1]),
+                     Ic=np.array(self.Ic[b0:b1]), vert_off=(vo[b0:b1 + 1] - vo[b0]).astype(np.int32),
+                     rest=np.array(self.rest[vo[b0]:vo[b1]]), edge_off=(eo[b0:b1 + 1] - eo[b0]).astype(np.int32),
+                     edges=np.array(self.edges[eo[b0]:eo[b1]]), face_off=(fo[b0:b1 + 1] - fo[b0]).astype(np.int32),
+                     faces=np.array(self.faces[fo[b0]:fo[b1]]), scene_id=None)
+
+    def scene_ranges(self):
+        """(first body, end body) of each scene, in order (one range without scene ids)."""
+        if self.scene_id is None:
+            return [(0, self.n_bodies)]
+        sid = np.asarray(self.scene_id)
+        cuts = [0] + [int(i) for i in np.nonzero(sid[1:] != sid[:-1])[0] + 1] + [self.n_bodies]
+        return list(zip(cuts[:-1], cuts[1:]))
+
 
 class SceneBuilder:
     def __init__(self):

@@ -12,7 +12,8 @@ every timed frame carries the full contact load. A step is one frame
 gb300 arm: W untimed frames, then K frames timed with CUDA events on the engine's
 stream (value, state resident in HBM), then the same K frames again through the public
 C ABI with host buffers (e2e: pinned host state -> device, step, device -> host every
-frame), then one profiled pass for the per-kernel roofline. N > 1 runs N independent
+frame), then one profiled pass (up to 5 frames) for the per-kernel roofline. The CPU
+baseline times the oracle on the first Newton iterations of the first timed frame. N > 1 runs N independent
 replicas (one per GPU; the pile does not shard): value = total frames/s of all ranks
 over the max-over-ranks time.
 reference arm: the CPU restatement of the reference (oracle/, OpenMP on all host
@@ -62,7 +63,7 @@ class ClockSampler:
     def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-             "clocks_event_reasons.sw_power_cap")
+             "clocks_event_reasons.sw_power_cap,memory.used")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -94,8 +95,10 @@ class ClockSampler:
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        mem = [float(s[7]) for s in self.samples if len(s) > 7 and s[7].replace(".", "").isdigit()]
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(self.samples),
+                "mem_used_gib": round(max(mem) / 1024.0, 2) if mem else None}
 
 
 def measured_peaks():
@@ -120,21 +123,69 @@ def ncu_traffic_per_unit(kernel):
     return None
 
 
-def cpu_baseline_frames(sc, cfg, q0, qd, frames_budget_s=90.0, max_frames=3):
-    """The CPU restatement on all host cores, one frame at a time from the checkpoint."""
+def batched_vs_looped(frames=3, warm_frames=10, n_scenes=256):
+    """The batched half of the metric: 256 independent scenes stepped in one handle
+    against the same scenes stepped one handle at a time, from the same state, at the same
+    Newton tolerance. Both sides are timed on the wall clock around the step calls (every
+    step call ends with a stream synchronisation); the final states are compared bit for
+    bit."""
+    from adb_gb300 import scene as S
+    from adb_gb300.abd import ABD
+    sc = S.batched_scenes(n_scenes=n_scenes, seed=0)
+    cfg = S.workload_config("batched")
+    bat = ABD(sc, cfg)
+    bat.step(warm_frames)                     # falling bodies reach their first contacts
+    q0, qd = bat.state()
+    it0 = bat.scene_stats()["iter"].copy()
+    t0 = time.perf_counter()
+    bst = bat.step(frames)
+    t_bat = time.perf_counter() - t0
+    bq, bqd = bat.state()
+    ranges = sc.scene_ranges()
+    handles = []
+    for k, (b0, b1) in enumerate(ranges):
+        h = ABD(sc.body_range(b0, b1), cfg)
+        h.set_state(q0[b0:b1], qd[b0:b1])
+        h.iter = int(it0[k])
+        handles.append(h)
+    t0 = time.perf_counter()
+    for h in handles:
+        h.step(frames)
+    t_loop = time.perf_counter() - t0
+    same = True
+    for h, (b0, b1) in zip(handles, ranges):
+        q, qdd = h.state()
+        same = same and bool(np.array_equal(q, bq[b0:b1]) and np.array_equal(qdd, bqd[b0:b1]))
+        h.close()
+    bat.close()
+    return {"scenes": len(ranges), "bodies": sc.n_bodies, "vertices": sc.n_vertices, "frames": frames,
+            "start": "frame %d of the seeded batch" % warm_frames,
+            "batched_scenes_per_s": len(ranges) * frames / t_bat,
+            "looped_scenes_per_s": len(ranges) * frames / t_loop,
+            "speedup": t_loop / t_bat, "bitwise_equal_to_looped": same,
+            "newton_iters": bst.newton_iters, "max_pt": bst.n_pt, "max_ee": bst.n_ee}
+
+
+def cpu_baseline_sample(sc, cfg, q0, qd, newton_per_frame, sample_iters=6):
+    """The CPU restatement on all host cores, timed on a bounded sample of one frame.
+
+    The sample is the first `sample_iters` Newton iterations (each with its line search and
+    re-culls) of the frame that starts from (q0, qd); frames/s is scaled from the time per
+    Newton iteration by the Newton iterations per frame the GPU run took on the same frames
+    (the two paths take identical iteration counts, which the parity tests check)."""
+    import dataclasses
     from oracle import oracle as O
     cores = os.cpu_count() or 1
-    sim = O.OracleSim(sc, cfg, n_threads=cores)
+    c2 = dataclasses.replace(cfg, max_iter=sample_iters)
+    sim = O.OracleSim(sc, c2, n_threads=cores)
     sim.set_state(q0, qd)
+    sim.iter = 0
     t0 = time.perf_counter()
-    n = 0
-    while n < max_frames:
-        st = sim.step(1)
-        n += 1
-        if st.status != 0 or time.perf_counter() - t0 > frames_budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return n / dt, cores, n, dt
+    st = sim.step(1)
+    secs = time.perf_counter() - t0
+    its = st.newton_iters
+    per_it = secs / max(its, 1)
+    return 1.0 / (per_it * newton_per_frame), cores, its, secs
 
 
 def run_reference(args):
@@ -146,7 +197,7 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     sim = O.OracleSim(sc, cfg, n_threads=cores)
     sim.set_state(q0, qd)
-    budget = float(os.environ.get("ABD_REF_BUDGET_S", "150"))
+    budget = float(os.environ.get("ABD_REF_BUDGET_S", "100"))
     t0 = time.perf_counter()
     n = 0
     # each step is one frame; the run stops at the time budget (at least one frame)
@@ -237,7 +288,7 @@ def run_gb300(args):
     # ---- per-kernel device time (separate profiled pass over the same frames) ----
     sim.set_state(start_q, start_qd)
     sim.profile(True)
-    pst = sim.step(args.steps)
+    pst = sim.step(min(args.steps, 5))
     kt = sim.kernel_times()
     sim.profile(False)
     tot = sum(v["ms"] for v in kt.values())
@@ -275,10 +326,14 @@ def run_gb300(args):
             "kernel_ms": {k: round(v["ms"], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1]["ms"])
                           if v["ms"] > 0},
         }
+        if not args.no_batched:
+            line["batched"] = batched_vs_looped()
         if world == 1 and not args.no_cpu_baseline:
-            v, cores, n, secs = cpu_baseline_frames(sc, cfg, start_q, start_qd, frames_budget_s=60.0, max_frames=1)
+            npf = st.newton_iters / max(args.steps, 1)
+            v, cores, its, secs = cpu_baseline_sample(sc, cfg, start_q, start_qd, npf)
             line["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": cores, "kind": "port",
-                                    "sample": "%d frame of the pile from the same state (%.1f s)" % (n, secs)}
+                                    "sample": ("first %d Newton iterations of the first timed frame (%.1f s), "
+                                               "scaled by %.2f Newton iterations per frame" % (its, secs, npf))}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -292,6 +347,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

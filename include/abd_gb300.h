@@ -73,7 +73,10 @@ typedef struct {
   const int* face_off;         /* n_bodies + 1 */
   const int* faces;            /* face_off[n] * 3, local vertex ids */
   const int* scene_id;         /* n_bodies or NULL: bodies of different scenes never touch;
-                                  bodies of one scene must be contiguous */
+                                  bodies of one scene must be contiguous. Each scene runs
+                                  its own Newton loop, CCD bound and line search, exactly as
+                                  if it were stepped alone (the batched mode; the reference
+                                  steps one scene per ABD object). */
 } abd_scene_desc;
 
 typedef struct {
@@ -100,9 +103,16 @@ int abd_step(abd_handle* h, double dt, int n_frames, abd_frame_stats* stats);
 int abd_get_state(abd_handle* h, double* q0, double* qdot);
 int abd_set_state(abd_handle* h, const double* q0, const double* qdot);
 int abd_get_counts(abd_handle* h, int* n_bodies, int* n_vertices, int* n_edges, int* n_faces);
-/* Cumulative Newton counter (the reference's ABD::iter, model/abd.h:53). */
+/* Cumulative Newton counter (the reference's ABD::iter, model/abd.h:53); of scene 0 for
+ * abd_get_iter, of every scene for abd_set_iter. */
 int abd_get_iter(abd_handle* h);
 int abd_set_iter(abd_handle* h, int iter);
+/* Batched mode (no reference counterpart: the reference steps one scene per ABD object).
+ * Number of scenes of the handle, and per-scene counts (arrays of that length, any may be
+ * NULL) accumulated over the frames of the last abd_step call, plus each scene's
+ * cumulative Newton counter. */
+int abd_get_scene_count(abd_handle* h);
+int abd_get_scene_stats(abd_handle* h, int* newton_iters, int* ls_trials, int* pcg_iters, int* iter);
 const char* abd_last_error(abd_handle* h);
 void abd_destroy(abd_handle* h);
 /* Per-kernel device timing: when enabled, every kernel of the step is bracketed with

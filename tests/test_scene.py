@@ -69,3 +69,17 @@ def test_generators_shapes():
     b = S.batched_scenes(6, seed=1)
     assert len(set(b.scene_id.tolist())) == 6
     assert np.all(np.diff(b.scene_id) >= 0)
+
+
+def test_scene_ranges_and_body_range():
+    sc = S.batched_scenes(n_scenes=5, seed=2, lo=2, hi=6)
+    ranges = sc.scene_ranges()
+    assert len(ranges) == 5 and ranges[0][0] == 0 and ranges[-1][1] == sc.n_bodies
+    assert all(a < b for a, b in ranges) and all(ranges[i][1] == ranges[i + 1][0] for i in range(4))
+    b0, b1 = ranges[2]
+    sub = sc.body_range(b0, b1)
+    assert sub.n_bodies == b1 - b0 and sub.scene_id is None
+    assert np.array_equal(sub.q0, sc.q0[b0:b1])
+    assert np.array_equal(sub.rest, sc.rest[sc.vert_off[b0]:sc.vert_off[b1]])
+    assert sub.vert_off[0] == 0 and sub.vert_off[-1] == sub.rest.shape[0]
+    assert sub.faces.max() < (sub.vert_off[1:] - sub.vert_off[:-1]).max()
