@@ -16,7 +16,8 @@ _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
 
 STATUS = {0: "ABD_OK", 1: "ABD_ERR_NAN", 2: "ABD_ERR_LS_STALL", 3: "ABD_ERR_PAIR_OVERFLOW", 4: "ABD_ERR_TOI_TINY",
-          5: "ABD_ERR_NOT_SPD", 6: "ABD_ERR_PCG_NOCONV", 7: "ABD_ERR_CUDA", 8: "ABD_ERR_INVALID", 9: "ABD_ERR_IO"}
+          5: "ABD_ERR_NOT_SPD", 6: "ABD_ERR_PCG_NOCONV", 7: "ABD_ERR_CUDA", 8: "ABD_ERR_INVALID", 9: "ABD_ERR_IO",
+          10: "ABD_ERR_SAME_DIRECTION"}
 
 
 class AbdConfig(C.Structure):
@@ -24,7 +25,10 @@ class AbdConfig(C.Structure):
         "dt", "kappa", "dhat", "ortho_kappa", "ground_offset", "mu", "evh", "eps_x", "backoff", "c1", "tol",
         "max_uk", "gravity_y", "ls_grad_tol", "pcg_rel_tol")] + [(n, C.c_int) for n in (
             "max_iter", "ground", "pt", "ee", "psd", "line_search", "upper_bound", "vg_fric", "pt_fric", "ee_fric",
-            "clip", "pcg_max_iter")]
+            "clip", "pcg_max_iter", "iaabb", "full_ccd")] + [(n, C.c_double) for n in (
+                "safe_factor", "sh_min_xyz", "sh_dx")] + [(n, C.c_int) for n in (
+                    "sh_xyz_bits", "sh_fix_edge_trajectory")] + [("dq_tol", C.c_double), ("damping", C.c_int),
+                                                                 ("damp_alpha", C.c_double), ("damp_beta", C.c_double)]
 
 
 class AbdSceneDesc(C.Structure):

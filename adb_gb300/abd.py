@@ -27,6 +27,10 @@ def make_abd_config(cfg: Config) -> L.AbdConfig:
     c.line_search, c.upper_bound = int(cfg.line_search), int(cfg.upper_bound)
     c.vg_fric, c.pt_fric, c.ee_fric = int(cfg.vg_friction), int(cfg.pt_friction), int(cfg.ee_friction)
     c.clip, c.pcg_max_iter = int(cfg.clip), int(cfg.pcg_max_iter)
+    c.iaabb, c.full_ccd, c.safe_factor = int(cfg.iaabb), int(cfg.full_ccd), cfg.safe_factor
+    c.sh_min_xyz, c.sh_dx, c.sh_xyz_bits = cfg.sh_min_xyz, cfg.sh_dx, int(cfg.sh_bits)
+    c.sh_fix_edge_trajectory, c.dq_tol = int(cfg.sh_fix_edge_trajectory), cfg.dq_tol
+    c.damping, c.damp_alpha, c.damp_beta = int(cfg.damping), cfg.damp_alpha, cfg.damp_beta
     return c
 
 

@@ -42,6 +42,8 @@ struct DBuf {
 };
 
 // Read-only geometry and state pointers passed by value to the kernels.
+struct Geo;
+__host__ __device__ inline bool scene_on(const Geo& g, int body);
 struct Geo {
   int nb, nv, ne, nf;
   const int *v_off, *e_off, *f_off;     // nb + 1
@@ -57,9 +59,15 @@ struct Geo {
   const int* bscene;                    // nb: scene of each body
   const int *sc_beg, *sc_end;           // ns: body range of each scene
   const double* alpha_s;                // ns or null: per-scene step for positions at q + alpha dq
+  const int* sc_act;                    // ns or null: scenes to process (culls, pair terms, energies);
+                                        // the others get no pairs and identity blocks
   const double *q, *dq, *q0, *dqdt;     // nb * 12
   double *X, *Xq, *X0;                  // 3 * nv, structure of arrays (x | y | z)
 };
+
+__host__ __device__ inline bool scene_on(const Geo& g, int body) {
+  return !g.sc_act || g.sc_act[g.bscene[body]] != 0;
+}
 
 // A culled pair set together with the overlap structure it was built on.
 struct PairSet {
@@ -80,7 +88,9 @@ struct PairSet {
 struct Params {
   double dhat, kappa, d_sqrt, eps_x, ortho_kappa, ground_offset, dt, gravity_y;
   double mu, epsv, max_uk;
+  double damp_alpha, damp_beta;  // "damping": {alpha, beta}
   int psd, pt_fric, ee_fric, vg_fric, ground, pt, ee;
+  int damp;                      // "damping": {enable}
 };
 
 // Culling scratch shared by all culls of a handle.
@@ -111,9 +121,9 @@ struct CullScratch {
 // profiling is on, brackets it with CUDA events on its stream so that each kernel's
 // device time is measured live.
 enum KTag {
-  K_PROJECT, K_BODY_BOXES, K_OV_COUNT, K_OV_FILL, K_OV_LOWER, K_PRIM_BOXES, K_BIN, K_CAND_COUNT, K_NARROW_FLAGS,
+  K_PROJECT, K_BODY_BOXES, K_OV_COUNT, K_OV_FILL, K_OV_LOWER, K_PRIM_BOXES, K_BIN, K_NARROW_SCAN,
   K_NARROW_WRITE, K_NARROW_TOI, K_VG, K_VG_TOI, K_SCAN, K_PAIR_TERMS, K_SEG, K_OV_REDUCE, K_BODY_SYSTEM,
-  K_BLOCK_INVERSE, K_PCG, K_ENERGY, K_DOTS, K_VEC, K_NTAGS
+  K_BLOCK_INVERSE, K_PCG, K_ENERGY, K_DOTS, K_VEC, K_SH, K_SORT, K_NTAGS
 };
 extern const char* const kTagNames[K_NTAGS];
 struct Prof {
@@ -164,6 +174,43 @@ void launch_project(const Geo& g, int which, double alpha, cudaStream_t s);
 void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs, PairSet& out, double* toi_p,
           double* toi_g, cudaStream_t s);
 
+// Vertex-ground pairs (d = (y + ground_offset)^2 < P.dhat) into S.vg / S.vg_seg.
+void vg_pairs(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, cudaStream_t s);
+// Ground times of impact of all vertices into the ground slots of the per-scene keys.
+void launch_vg_toi(const Geo& g, const Params& P, unsigned long long* toi_key, cudaStream_t s);
+
+// ---------------- sort (sort.cu) ----------------
+size_t sort_padded_size(size_t n);  // buffer size sort_u64 needs for n keys
+void sort_u64(unsigned long long* keys, size_t n, size_t cap, cudaStream_t s);
+
+// ---------------- spatial-hash broad phase (shash.cu) ----------------
+struct ShParams {
+  double min_xyz, dx, safe_factor;
+  int bits, fix_edge, full_ccd;
+};
+struct ShTable {
+  DBuf<long long> cnt, off, scan_tmp;
+  DBuf<unsigned long long> keys;
+  DBuf<int> bstart, bend;
+  long long n = 0;
+  long long h_tot = 0;
+};
+struct ShScratch {
+  ShTable tab;
+  DBuf<int> qcnt, qoff, scan_i, flag, pos;
+  DBuf<unsigned long long> pt_keys, ee_keys, bp_all, tkeys;
+  DBuf<unsigned> bp_pt, bp_ee;
+  int* h_int = nullptr;
+  unsigned long long* h_toi = nullptr;
+  int h_toi_cap = 0;
+};
+// gen_collision_set: pair set of the configuration at q (vtn 1) or q + alpha dq (vtn 2).
+void sh_cull(const Geo& g, const Params& P, const ShParams& H, int vtn, double alpha, ShScratch& W, CullScratch& cs,
+             PairSet& S, cudaStream_t s);
+// step_size_upper_bound: per-scene bound of the step q -> q + dq into toi (host, g.ns).
+void sh_bound(const Geo& g, const Params& P, const ShParams& H, const PairSet& cur, ShScratch& W, CullScratch& cs,
+              double* toi, cudaStream_t s);
+
 // ---------------- Newton system (newton.cu) ----------------
 enum { CONTRIB = 456 };  // dI(144) dJ(144) off(144) gI(12) gJ(12)
 struct NewtonBufs {
@@ -194,6 +241,9 @@ void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet&
             NewtonBufs& nb, cudaStream_t s, double* out);
 // Per scene over its 12 n dofs: out[3s] = dq.grad, out[3s+1] = |grad|^2, out[3s+2] = |dq|^2
 void dots(const Geo& g, const double* dq, const double* grad, NewtonBufs& nb, double* out, cudaStream_t s);
+// Per scene: out[3s] = a.b, out[3s+1] = |b|^2, out[3s+2] = |a - b|^2
+void scene_diff(const Geo& g, const double* a, const double* b, NewtonBufs& nb, double* out, cudaStream_t s);
+void launch_copy_scene(const Geo& g, double* dst, const double* src, const int* on, cudaStream_t st);
 void launch_scale_scene(const Geo& g, double* v, const double* f, cudaStream_t st);
 void launch_q_update_scene(const Geo& g, double* q, const double* dq, const double* alpha, cudaStream_t st);
 void launch_frame_end(double* q, double* q0, double* dqdt, int n, double dt, cudaStream_t st);

@@ -82,6 +82,10 @@ __global__ void k_ov_count(Geo g, const double* bbox, int* cnt_all, int* cnt_up)
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= g.nb) return;
   int i = warp;
+  if (!scene_on(g, i)) {
+    if (lane == 0) cnt_all[i] = cnt_up[i] = 0;
+    return;
+  }
   box bi = ldbox(bbox, i);
   int ca = 0, cu = 0;
   for (int j0 = g.scene_beg[i]; j0 < g.scene_end[i]; j0 += 32) {
@@ -107,6 +111,7 @@ __global__ void k_ov_fill(Geo g, const double* bbox, const int* row_ptr, const i
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= g.nb) return;
   int i = warp;
+  if (!scene_on(g, i)) return;
   box bi = ldbox(bbox, i);
   int pa = row_ptr[i], pu = up_ptr[i];
   unsigned below = (1u << lane) - 1u;
@@ -252,8 +257,10 @@ __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const 
 }
 
 constexpr int NT = 256;     // narrow-phase threads per CTA
-constexpr int TILE = 512;   // primitives of one list staged in shared memory (2 x 12 kB)
+constexpr int TILE = 384;   // primitives of one list staged in shared memory (2 x 9 kB)
 constexpr int REC_CAP = 2048;  // accepted pairs of one overlap kept in shared memory for sorting
+constexpr int STEP = 8;     // box-phase candidates per thread between two exact phases
+constexpr int QCAP = NT * STEP;  // queue of float-box hits (8 kB)
 
 __device__ __forceinline__ void finflate(const float* s, float ds, float* o) {
   o[0] = __fsub_rd(s[0], ds); o[1] = __fsub_rd(s[1], ds); o[2] = __fsub_rd(s[2], ds);
@@ -361,25 +368,39 @@ __device__ __forceinline__ bool f_hit(const float* a, const float* b) {
 
 // 5a. Narrow phase, one CTA per overlap, count (MODE 0) or trajectory TOI (MODE 2).
 // For each sub-problem (v(I) x f(J), v(J) x f(I), e(I) x e(J)) the float boxes of both
-// lists are staged in shared memory; each thread keeps one A box in registers and walks
-// the B boxes (a shared-memory broadcast per step); survivors get the exact test.
+// lists are staged in shared memory. The work alternates between two phases so that the
+// FP64 work is spread evenly over the CTA:
+//  - box phase: each thread keeps one A box in registers and walks its B boxes (a
+//    shared-memory broadcast per step), STEP candidates per thread, and appends the
+//    float-box hits to a shared queue (warp-aggregated);
+//  - exact phase: the whole CTA takes the queued candidates round-robin for the exact
+//    FP64 test (MODE 0: box, lower bounds, type and distance; MODE 2: time of impact).
 template <int MODE>
-__global__ void __launch_bounds__(NT) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
+__global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
                                                     const int* cnt, const int* off, const int* lst, const float* vb,
                                                     const float* eb, const float* fb, int* sub_cnt,
                                                     unsigned long long* toi_key, unsigned long long* stage_key,
                                                     int8_t* stage_ty, int* stage_off, int* stage_total,
                                                     int stage_cap) {
   __shared__ float sA[TILE * 6], sB[TILE * 6];
+  __shared__ unsigned int sq[QCAP];
+  __shared__ int sq_n[2];
   __shared__ unsigned long long recK[MODE == 0 ? REC_CAP : 1];
   __shared__ int8_t recT[MODE == 0 ? REC_CAP : 1];
   __shared__ int rec_n, rec_base;
   const int u = blockIdx.x;
   const int* n = cnt + 6 * u;
   const int* o = off + 6 * u;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
   int c3s[3] = {0, 0, 0};
   double tmin = 1.0;
-  if (MODE == 0 && threadIdx.x == 0) rec_n = 0;
+  if (threadIdx.x == 0) {
+    rec_n = 0;
+    sq_n[0] = 0;
+    sq_n[1] = 0;
+  }
+  int par = 0;
 #pragma unroll 1
   for (int sub = 0; sub < 3; ++sub) {
     SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, o, lst, vb, eb, fb);
@@ -387,48 +408,85 @@ __global__ void __launch_bounds__(NT) k_narrow_scan(Geo g, Params P, float ds_f,
     int cs = 0;
 #pragma unroll 1
     for (int a0 = 0; a0 < L.nA; a0 += TILE) {
-      int ca = min(TILE, L.nA - a0);
+      const int ca = min(TILE, L.nA - a0);
 #pragma unroll 1
       for (int b0 = 0; b0 < L.nB; b0 += TILE) {
-        int cb = min(TILE, L.nB - b0);
+        const int cb = min(TILE, L.nB - b0);
         stage(L, a0, ca, b0, cb, MODE != 2, ds_f, sA, sB);
-        // thread t: row i = t mod ca, columns j = t / ca + q * (NT / ca) (rows >= NT: stride)
-        int phases = ca >= NT ? 1 : NT / ca;
-        int row0 = threadIdx.x % (ca < NT ? ca : NT);
-        int ph = ca < NT ? threadIdx.x / ca : 0;
-        if (ph < phases) {
-#pragma unroll 1
-          for (int i = row0; i < ca; i += (ca < NT ? ca : NT)) {
-            float a[6];
+        // thread t: rows i = t mod ca (ca < NT) or t, t + NT, ... (ca >= NT); columns
+        // j = ph, ph + phases, ... with phases = NT / ca threads sharing a row
+        const int rows = ca < NT ? ca : NT;
+        const int phases = ca < NT ? NT / ca : 1;
+        const int ph = ca < NT ? threadIdx.x / ca : 0;
+        const int row0 = threadIdx.x % rows;
+        const bool live = ph < phases;
+        const int ncol = live ? (cb - ph + phases - 1) / phases : 0;        // columns per row
+        const int nrow = (live && ncol > 0) ? (ca - row0 + rows - 1) / rows : 0;  // rows of this thread
+        const int max_items = (ca < NT ? 1 : (ca + NT - 1) / NT) * ((cb + phases - 1) / phases);
+        const int steps = (max_items + STEP - 1) / STEP;
+        int ri = 0, cj = 0;  // cursor: row index (of this thread's rows), column index
+        float a[6];
+        if (nrow > 0)
 #pragma unroll
-            for (int c = 0; c < 6; ++c) a[c] = sA[6 * i + c];
-            int pa = L.offA + L.LA[a0 + i];
+          for (int c = 0; c < 6; ++c) a[c] = sA[6 * row0 + c];
 #pragma unroll 1
-            for (int j = ph; j < cb; j += phases) {
-              if (!f_hit(a, sB + 6 * j)) continue;
-              int pb = L.offB + L.LB[b0 + j];
-              if (MODE == 2) {
-                tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
-              } else {
-                int f = exact_pair(g, P, sub, pa, pb);
-                if (f) {
-                  ++cs;
-                  int slot = atomicAdd(&rec_n, 1);
-                  if (slot < REC_CAP) {
-                    recK[slot] = ((unsigned long long)sub << 60) | ((unsigned long long)(a0 + i) << 30) |
-                                 (unsigned long long)(b0 + j);
-                    recT[slot] = (int8_t)(f - 1);
-                  }
+        for (int st = 0; st < steps; ++st) {
+          // box phase
+#pragma unroll 1
+          for (int it = 0; it < STEP; ++it) {
+            bool hit = false;
+            unsigned code = 0;
+            if (ri < nrow) {
+              int i = row0 + ri * rows, j = ph + cj * phases;
+              hit = i < ca && j < cb && f_hit(a, sB + 6 * j);
+              code = ((unsigned)i << 16) | (unsigned)j;
+              if (++cj == ncol) {
+                cj = 0;
+                if (++ri < nrow)
+#pragma unroll
+                  for (int c = 0; c < 6; ++c) a[c] = sA[6 * (row0 + ri * rows) + c];
+              }
+            }
+            unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (m) {
+              int base = 0;
+              if (lane == 0) base = atomicAdd(&sq_n[par], __popc(m));
+              base = __shfl_sync(0xffffffffu, base, 0);
+              if (hit) sq[base + __popc(m & below)] = code;
+            }
+          }
+          __syncthreads();
+          // exact phase
+          const int nq = sq_n[par];
+          if (threadIdx.x == 0) sq_n[par ^ 1] = 0;
+#pragma unroll 1
+          for (int k = threadIdx.x; k < nq; k += NT) {
+            unsigned code = sq[k];
+            int i = (int)(code >> 16), j = (int)(code & 0xffffu);
+            if (i >= ca || j >= cb) continue;
+            int pa = L.offA + L.LA[a0 + i], pb = L.offB + L.LB[b0 + j];
+            if (MODE == 2) {
+              tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
+            } else {
+              int f = exact_pair(g, P, sub, pa, pb);
+              if (f) {
+                ++cs;
+                int slot = atomicAdd(&rec_n, 1);
+                if (slot < REC_CAP) {
+                  recK[slot] = ((unsigned long long)sub << 60) | ((unsigned long long)(a0 + i) << 30) |
+                               (unsigned long long)(b0 + j);
+                  recT[slot] = (int8_t)(f - 1);
                 }
               }
             }
           }
+          par ^= 1;
+          __syncthreads();
         }
       }
     }
     c3s[sub] = cs;
   }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (MODE == 0) {
     __shared__ int sh[3][NT / 32];
 #pragma unroll
@@ -524,15 +582,15 @@ __global__ void k_narrow_copy(int nov, const int* ovI, const int* ovJ, const int
   }
 }
 
-// 5b. Ordered write. Sub-problems without pairs are skipped; each (i, j) chunk is walked
-// in row-major order with a CTA-wide ordered compaction, stopping once the sub-problem's
-// count (from the count pass) has been written.
+// 5b. Ordered write for the overlaps whose pairs did not fit the shared-memory sort. The
+// (i, j) space of each sub-problem is walked in row-major order (the order of the
+// reference's nested loops), NT candidates at a time, with a CTA-wide ordered
+// compaction, stopping once the sub-problem's count (from the count pass) is written.
 __global__ void __launch_bounds__(NT) k_narrow_write(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
                                                      const int* cnt, const int* off, const int* lst, const float* vb,
                                                      const float* eb, const float* fb, const int* sub_cnt,
                                                      const int* ov_pt_off, const int* ov_ee_off, NarrowOut out,
                                                      const int* stage_off) {
-  __shared__ float sA[TILE * 6], sB[TILE * 6];
   __shared__ int wcnt[NT / 32];
   const int u = blockIdx.x;
   const int* sc = sub_cnt + 3 * u;
@@ -546,48 +604,41 @@ __global__ void __launch_bounds__(NT) k_narrow_write(Geo g, Params P, float ds_f
   for (int sub = 0; sub < 3; ++sub) {
     if (sc[sub] == 0) continue;
     SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, o, lst, vb, eb, fb);
-    int need = sc[sub], done = 0;
+    const int need = sc[sub];
+    int done = 0;
+    const long long tot = (long long)L.nA * L.nB;
 #pragma unroll 1
-    for (int a0 = 0; a0 < L.nA && done < need; a0 += TILE) {
-      int ca = min(TILE, L.nA - a0);
-#pragma unroll 1
-      for (int b0 = 0; b0 < L.nB && done < need; b0 += TILE) {
-        int cb = min(TILE, L.nB - b0);
-        stage(L, a0, ca, b0, cb, true, ds_f, sA, sB);
-        const int tot = ca * cb;
-#pragma unroll 1
-        for (int k0 = 0; k0 < tot && done < need; k0 += NT) {
-          int k = k0 + threadIdx.x;
-          int f = 0, i = 0, j = 0;
-          if (k < tot) {
-            i = k / cb;
-            j = k - i * cb;
-            if (f_hit(sA + 6 * i, sB + 6 * j))
-              f = exact_pair(g, P, sub, L.offA + L.LA[a0 + i], L.offB + L.LB[b0 + j]);
-          }
-          unsigned m = __ballot_sync(0xffffffffu, f != 0);
-          if (lane == 0) wcnt[w] = __popc(m);
-          __syncthreads();
-          int pre = 0, total = 0;
-#pragma unroll
-          for (int q = 0; q < NT / 32; ++q) {
-            pre += (q < w) ? wcnt[q] : 0;
-            total += wcnt[q];
-          }
-          if (f) {
-            int idx = (sub < 2 ? run_pt : run_ee) + pre + __popc(m & below);
-            int la_id = L.LA[a0 + i], lb_id = L.LB[b0 + j];
-            int* dst = sub < 2 ? out.pt : out.ee;
-            dst[4 * idx] = L.A; dst[4 * idx + 1] = la_id; dst[4 * idx + 2] = L.B; dst[4 * idx + 3] = lb_id;
-            (sub < 2 ? out.pt_ty : out.ee_ty)[idx] = (int8_t)(f - 1);
-            (sub < 2 ? out.pt_ov : out.ee_ov)[idx] = u;
-          }
-          if (sub < 2) run_pt += total;
-          else run_ee += total;
-          done += total;
-          __syncthreads();
-        }
+    for (long long k0 = 0; k0 < tot && done < need; k0 += NT) {
+      long long k = k0 + threadIdx.x;
+      int f = 0, i = 0, j = 0;
+      if (k < tot) {
+        i = (int)(k / L.nB);
+        j = (int)(k - (long long)i * L.nB);
+        float a[6];
+        finflate(L.boxA + 6 * (L.offA + L.LA[i]), ds_f, a);
+        if (f_hit(a, L.boxB + 6 * (L.offB + L.LB[j])))
+          f = exact_pair(g, P, sub, L.offA + L.LA[i], L.offB + L.LB[j]);
       }
+      unsigned m = __ballot_sync(0xffffffffu, f != 0);
+      if (lane == 0) wcnt[w] = __popc(m);
+      __syncthreads();
+      int pre = 0, total = 0;
+#pragma unroll
+      for (int q = 0; q < NT / 32; ++q) {
+        pre += (q < w) ? wcnt[q] : 0;
+        total += wcnt[q];
+      }
+      if (f) {
+        int idx = (sub < 2 ? run_pt : run_ee) + pre + __popc(m & below);
+        int* dst = sub < 2 ? out.pt : out.ee;
+        dst[4 * idx] = L.A; dst[4 * idx + 1] = L.LA[i]; dst[4 * idx + 2] = L.B; dst[4 * idx + 3] = L.LB[j];
+        (sub < 2 ? out.pt_ty : out.ee_ty)[idx] = (int8_t)(f - 1);
+        (sub < 2 ? out.pt_ov : out.ee_ov)[idx] = u;
+      }
+      if (sub < 2) run_pt += total;
+      else run_ee += total;
+      done += total;
+      __syncthreads();
     }
   }
 }
@@ -604,7 +655,7 @@ __global__ void k_vg_count(Geo g, Params P, int* blk_cnt) {
   __shared__ int sh[32];
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   bool hit = false;
-  if (v < g.nv) {
+  if (v < g.nv && scene_on(g, g.vbody[v])) {
     double d = XA(g.X[g.nv + v], P.ground_offset);
     d = XM(d, d);
     hit = d < P.dhat;
@@ -622,7 +673,7 @@ __global__ void k_vg_write(Geo g, Params P, const int* blk_off, int* vg) {
   __shared__ int sh[32];
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   bool hit = false;
-  if (v < g.nv) {
+  if (v < g.nv && scene_on(g, g.vbody[v])) {
     double d = XA(g.X[g.nv + v], P.ground_offset);
     d = XM(d, d);
     hit = d < P.dhat;
@@ -657,7 +708,7 @@ __global__ void k_vg_seg(int nb, int nvg, const int* vg, int* seg) {
 // of scene 0 (slots alternate pt/ee, ground per scene).
 __global__ void k_vg_toi(Geo g, Params P, unsigned long long* toi_key) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= g.nv) return;
+  if (v >= g.nv || !scene_on(g, g.vbody[v])) return;
   double d2 = XA(g.X[g.nv + v], P.ground_offset);
   if (d2 < 0) {
     double d1 = XA(g.Xq[g.nv + v], P.ground_offset);
@@ -813,7 +864,7 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
     }
     for (int attempt = 0; attempt < 4; ++attempt) {
       CK(cudaMemsetAsync(d_tot + 6, 0, sizeof(int), s));
-      KLAUNCH(K_NARROW_FLAGS, s, k_narrow_scan<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
+      KLAUNCH(K_NARROW_SCAN, s, k_narrow_scan<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
                                                                       cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
                                                                       cs.fbox.p, cs.sub_cnt.p, nullptr, cs.stage_key.p,
                                                                       cs.stage_ty.p, cs.stage_off.p, d_tot + 6,
@@ -825,14 +876,14 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
       cs.stage_key.ensure((size_t)cs.h_small[6] + (cs.h_small[6] >> 2) + 1024);
       cs.stage_ty.ensure(cs.stage_key.cap);
     }
-    KLAUNCH(K_NARROW_FLAGS, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
+    KLAUNCH(K_NARROW_WRITE, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
     scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
     scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
     CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     npt = cs.h_small[3];
     nee = cs.h_small[4];
-    prof_work(K_NARROW_FLAGS, nov, 24.0 * g.nv + 20.0 * ((double)npt + nee));
+    prof_work(K_NARROW_SCAN, nov, 24.0 * g.nv + 20.0 * ((double)npt + nee));
     S.pt.ensure(4 * (size_t)npt + 4);
     S.pt_ty.ensure(npt + 1);
     S.pt_ov.ensure(npt + 1);
@@ -851,8 +902,19 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
   S.npt = npt;
   S.nee = nee;
   // 6. vertex-ground pairs
+  vg_pairs(g, P, cs, S, s);
+}
+
+void vg_pairs(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, cudaStream_t s) {
+  const int nb = g.nb;
   int nvg = 0;
   S.vg_seg.ensure(nb + 2);
+  cs.tmp_int.ensure(64);
+  int* d_tot = cs.tmp_int.p;
+  if (!cs.h_small) {
+    CK(cudaMallocHost(&cs.h_small, 64 * sizeof(int)));
+    CK(cudaMallocHost(&cs.h_ll, 8 * sizeof(long long)));
+  }
   if (P.ground && g.nv) {
     int nbv = nblk(g.nv, 256);
     cs.vflag_off.ensure(nbv + 1);
@@ -866,7 +928,13 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
     KLAUNCH(K_VG, s, k_vg_write<<<nbv, 256, 0, s>>>(g, P, cs.vflag_off.p, S.vg.p));
   }
   S.nvg = nvg;
+  S.vg.ensure(2);
   KLAUNCH(K_VG, s, k_vg_seg<<<nblk(nb + 1, 256), 256, 0, s>>>(nb, nvg, S.vg.p, S.vg_seg.p));
+}
+
+void launch_vg_toi(const Geo& g, const Params& P, unsigned long long* toi_key, cudaStream_t s) {
+  if (!g.nv) return;
+  KLAUNCH(K_VG_TOI, s, k_vg_toi<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, toi_key + 1));
 }
 
 }  // namespace abd

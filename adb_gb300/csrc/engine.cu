@@ -18,9 +18,9 @@ void check(cudaError_t e, const char* where) {
 }
 
 const char* const kTagNames[K_NTAGS] = {
-    "project", "body_boxes", "ov_count", "ov_fill", "ov_lower", "prim_boxes", "bin", "cand_count", "narrow_flags",
+    "project", "body_boxes", "ov_count", "ov_fill", "ov_lower", "prim_boxes", "bin", "narrow_scan",
     "narrow_write", "narrow_toi", "vg", "vg_toi", "scan", "pair_terms", "seg", "ov_reduce", "body_system",
-    "block_inverse", "pcg", "energy", "dots", "vec"};
+    "block_inverse", "pcg", "energy", "dots", "vec", "spatial_hash", "sort"};
 thread_local Prof* g_prof = nullptr;
 
 cudaEvent_t Prof::get() {
@@ -82,7 +82,7 @@ struct Engine {
   int nb = 0, nv = 0, ne = 0, nf = 0;
   cudaStream_t s = nullptr;
   DBuf<int> v_off, e_off, f_off, vbody, ev, fv, scene_beg, scene_end;
-  DBuf<double> rest, mass, Ic, rest_box, q, q0, dqdt, dq, X, Xq, X0;
+  DBuf<double> rest, mass, Ic, rest_box, q, q0, dqdt, dq, X, Xq, X0, lastdq;
   PairSet sets[3];
   int cur = 0;
   CullScratch cs;
@@ -91,12 +91,16 @@ struct Engine {
   // scenes: independent sub-problems, each with its own Newton loop, step bound and
   // line search (a single scene is the reference's ABD::implicit_euler)
   int ns = 1;
-  DBuf<int> bscene, sc_beg, sc_end, sc_on;
+  DBuf<int> bscene, sc_beg, sc_end, sc_on, sc_iter, sc_search;
   DBuf<double> sc_alpha, sc_factor;
   std::vector<int> h_sc_beg, h_sc_end;
   std::vector<int> iter, g_cnt, p_cnt;           // per scene (iter: cumulative, model/abd.h:53)
   std::vector<int> sc_newton, sc_ls, sc_pcg;     // per scene, over the last abd_step call
+  std::vector<char> has_lastdq;                  // per scene: lastdq holds a previous step
+  ShParams sh{};                                 // spatial-hash broad phase (iaabb even / <= 1)
+  ShScratch shw;
   int* h_on = nullptr;                           // pinned staging of per-scene uploads
+  int *h_iter = nullptr, *h_search = nullptr;
   double *h_alpha = nullptr, *h_factor = nullptr;
   std::string err;
   Prof prof;
@@ -109,15 +113,18 @@ struct Engine {
     g.mass = mass.p; g.Ic = Ic.p; g.rest_box = rest_box.p;
     g.scene_beg = scene_beg.p; g.scene_end = scene_end.p;
     g.ns = ns; g.bscene = bscene.p; g.sc_beg = sc_beg.p; g.sc_end = sc_end.p; g.alpha_s = nullptr;
+    g.sc_act = nullptr;
     g.q = q.p; g.dq = dq.p; g.q0 = q0.p; g.dqdt = dqdt.p;
     g.X = X.p; g.Xq = Xq.p; g.X0 = X0.p;
     return g;
   }
 
   ~Engine() {
-    DBuf<int>* ib[] = {&v_off, &e_off, &f_off, &vbody, &ev, &fv, &scene_beg, &scene_end, &bscene, &sc_beg, &sc_end, &sc_on};
+    DBuf<int>* ib[] = {&v_off,  &e_off,  &f_off,  &vbody, &ev,    &fv,      &scene_beg, &scene_end,
+                       &bscene, &sc_beg, &sc_end, &sc_on, &sc_iter, &sc_search};
     for (auto* b : ib) b->release();
-    DBuf<double>* db[] = {&rest, &mass, &Ic, &rest_box, &q, &q0, &dqdt, &dq, &X, &Xq, &X0, &sc_alpha, &sc_factor};
+    DBuf<double>* db[] = {&rest, &mass, &Ic, &rest_box, &q, &q0, &dqdt, &dq, &X, &Xq, &X0, &sc_alpha, &sc_factor,
+                          &lastdq};
     for (auto* b : db) b->release();
     for (auto& S : sets) {
       S.row_ptr.release(); S.col.release(); S.upidx.release(); S.ovI.release(); S.ovJ.release();
@@ -143,6 +150,8 @@ struct Engine {
     if (nbufs.h_red) cudaFreeHost(nbufs.h_red);
     if (nbufs.h_int) cudaFreeHost(nbufs.h_int);
     if (h_on) cudaFreeHost(h_on);
+    if (h_iter) cudaFreeHost(h_iter);
+    if (h_search) cudaFreeHost(h_search);
     if (h_alpha) cudaFreeHost(h_alpha);
     if (h_factor) cudaFreeHost(h_factor);
     if (s) cudaStreamDestroy(s);
@@ -174,6 +183,27 @@ struct Engine {
     P.ground = c->ground;
     P.pt = c->pt;
     P.ee = c->ee;
+    P.damp = c->damping;
+    P.damp_alpha = c->damp_alpha;
+    P.damp_beta = c->damp_beta;
+    sh.min_xyz = c->sh_min_xyz;
+    sh.dx = c->sh_dx;
+    sh.safe_factor = c->safe_factor;
+    sh.bits = c->sh_xyz_bits;
+    sh.fix_edge = c->sh_fix_edge_trajectory;
+    sh.full_ccd = c->full_ccd;
+    if (c->iaabb % 2 == 0 || (c->upper_bound && c->iaabb <= 1)) {
+      if (!(c->sh_dx > 0) || c->sh_xyz_bits < 1 || c->sh_xyz_bits > 9 || !(c->safe_factor > 0))
+        throw std::invalid_argument("spatial hashing: need dx > 0, 1 <= xyz_bits <= 9, safe_factor > 0");
+    }
+    if (c->iaabb % 2 == 0) {
+      // the reference's hash entries hold 16-bit body and primitive ids (spatial_hashing.h:9)
+      bool ok = d->n_bodies <= 32767;
+      for (int b = 0; ok && b < d->n_bodies; ++b)
+        ok = d->vert_off[b + 1] - d->vert_off[b] <= 32767 && d->edge_off[b + 1] - d->edge_off[b] <= 32767 &&
+             d->face_off[b + 1] - d->face_off[b] <= 32767;
+      if (!ok) throw std::invalid_argument("spatial hashing: at most 32767 bodies and 32767 primitives per body");
+    }
     CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     nb = d->n_bodies;
     nv = d->vert_off[nb];
@@ -241,6 +271,10 @@ struct Engine {
     sc_ls.assign(ns, 0);
     sc_pcg.assign(ns, 0);
     CK(cudaMallocHost(&h_on, ns * sizeof(int)));
+    CK(cudaMallocHost(&h_iter, ns * sizeof(int)));
+    CK(cudaMallocHost(&h_search, ns * sizeof(int)));
+    sc_iter.ensure(ns);
+    sc_search.ensure(ns);
     CK(cudaMallocHost(&h_alpha, ns * sizeof(double)));
     CK(cudaMallocHost(&h_factor, ns * sizeof(double)));
     upload(bscene, hbs.data(), nb);
@@ -266,6 +300,9 @@ struct Engine {
     upload(dqdt, d->dqdt, 12 * (size_t)nb);
     dq.ensure(12 * (size_t)nb);
     CK(cudaMemsetAsync(dq.p, 0, 12 * (size_t)nb * sizeof(double), s));
+    lastdq.ensure(12 * (size_t)nb);
+    CK(cudaMemsetAsync(lastdq.p, 0, 12 * (size_t)nb * sizeof(double), s));
+    has_lastdq.assign(ns, 0);
     X.ensure(3 * (size_t)nv + 3);
     Xq.ensure(3 * (size_t)nv + 3);
     X0.ensure(3 * (size_t)nv + 3);
@@ -281,11 +318,24 @@ struct Engine {
     return (20 + 96 + 96) * P_ + 200 * P_ + 2 * 1152.0 * (nb + 2.0 * S.nov) + 2 * 96.0 * nb;
   }
 
+  // Pair-set culling at q (vtn 1) or at q + alpha dq (vtn 2): iAABB for odd iaabb, the
+  // spatial hash for even (abd.cpp:48-51, line_search.cpp:88-110).
+  // Positions at q + alpha dq use the per-scene steps of g when it carries them.
+  void cull_set(const Geo& g, int vtn, PairSet& S, double alpha = 1.0) {
+    if (cfg.iaabb % 2) cull(g, P, vtn, alpha, cs, S, nullptr, nullptr, s);
+    else sh_cull(g, P, sh, vtn, alpha, shw, cs, S, s);
+  }
+
   // Uploads of per-scene values go through pinned staging arrays; every upload is followed
   // by a stream synchronisation before its staging array is written again.
   void put_on(const std::vector<char>& on) {
     for (int k = 0; k < ns; ++k) h_on[k] = on[k] ? 1 : 0;
     CK(cudaMemcpyAsync(sc_on.p, h_on, ns * sizeof(int), cudaMemcpyHostToDevice, s));
+  }
+  // masks of the scenes still iterating / still searching (culls, pair terms, energies)
+  void put_mask(DBuf<int>& d, int* h, const std::vector<char>& on) {
+    for (int k = 0; k < ns; ++k) h[k] = on[k] ? 1 : 0;
+    CK(cudaMemcpyAsync(d.p, h, ns * sizeof(int), cudaMemcpyHostToDevice, s));
   }
   void put_alpha(const std::vector<double>& a) {
     for (int k = 0; k < ns; ++k) h_alpha[k] = a[k];
@@ -310,22 +360,25 @@ struct Engine {
     launch_copy(q.p, q0.p, n12, s);
     CK(cudaMemsetAsync(dq.p, 0, n12 * sizeof(double), s));
     launch_project(g, 0, 0.0, s);
-    cull(g, P, 1, 0.0, cs, sets[cur], nullptr, nullptr, s);
+    cull_set(g, 1, sets[cur]);
     st.bytes_moved += bytes_cull(sets[cur]);
     std::vector<char> act(ns, 1), ls(ns, 0), stalled(ns, 0);
     std::vector<double> dd(3 * ns), sup_dq(ns), tp(ns, 1.0), tg(ns, 1.0), toi(ns, 1.0), fac(ns, 1.0);
     std::vector<double> E0(ns), E1(ns), qdg(ns), gn(ns), dqn(ns), a_cull(ns, 1.0), a_fin(ns, 1.0);
-    std::vector<int> trials(ns, 0), its_s(ns, 0);
+    std::vector<int> trials(ns, 0), its_s(ns, 0), fin_pass(ns, 0);
     int n_act = ns;
     int status = ABD_OK;
     while (n_act > 0) {
       auto t0 = clk::now();
       PairSet& S = sets[cur];
+      put_mask(sc_iter, h_iter, act);
+      Geo ga = g;  // the scenes still iterating
+      ga.sc_act = sc_iter.p;
       st.n_pt = std::max(st.n_pt, S.npt);
       st.n_ee = std::max(st.n_ee, S.nee);
       st.n_vg = std::max(st.n_vg, S.nvg);
       st.n_overlaps = std::max(st.n_overlaps, S.nov);
-      assemble(g, P, S, nbufs, s);
+      assemble(ga, P, S, nbufs, s);
       put_on(act);
       st.bytes_moved += bytes_assemble(S);
       auto t1 = clk::now();
@@ -344,8 +397,12 @@ struct Engine {
       auto t2 = clk::now();
       // CCD step bound (abd.cpp:142-196)
       for (int k = 0; k < ns; ++k) toi[k] = 1.0;
-      if (cfg.upper_bound) {
-        cull(g, P, 3, 1.0, cs, sets[2], tp.data(), tg.data(), s);
+      if (cfg.upper_bound && cfg.iaabb <= 1) {
+        // step_size_upper_bound (upper_bound.cpp:16-277)
+        sh_bound(ga, P, sh, S, shw, cs, toi.data(), s);
+        st.bytes_moved += 96.0 * nv;
+      } else if (cfg.upper_bound) {
+        cull(ga, P, 3, 1.0, cs, sets[2], tp.data(), tg.data(), s);
         st.bytes_moved += 96.0 * nv + 20.0 * sets[2].nov;
         for (int k = 0; k < ns; ++k) {
           if (!act[k]) continue;
@@ -359,6 +416,20 @@ struct Engine {
           if ((cfg.ground && g_cnt[k] > 1) || p_cnt[k] > 1) return ABD_ERR_TOI_TINY;
         }
       }
+      // same-direction stop (abd.cpp:180-190): with dq_tol <= 0 it can never trigger
+      if (cfg.dq_tol > 0) {
+        std::vector<double> df(3 * ns);
+        scene_diff(g, dq.p, lastdq.p, nbufs, df.data(), s);
+        for (int k = 0; k < ns; ++k) {
+          if (!act[k] || !iter[k] || !has_lastdq[k]) continue;
+          double c = df[3 * k] / (std::sqrt(dd[3 * k + 2]) * std::sqrt(df[3 * k + 1]));
+          if (std::fabs(c) > 1.0 - cfg.dq_tol && std::sqrt(df[3 * k + 2]) / std::sqrt(dd[3 * k + 2]) < cfg.dq_tol)
+            return ABD_ERR_SAME_DIRECTION;
+        }
+        launch_copy_scene(g, lastdq.p, dq.p, sc_on.p, s);
+        for (int k = 0; k < ns; ++k)
+          if (act[k]) has_lastdq[k] = 1;
+      }
       for (int k = 0; k < ns; ++k) {
         double factor = toi[k] < 1.0 ? cfg.backoff : 1.0;
         fac[k] = factor * toi[k];
@@ -371,7 +442,7 @@ struct Engine {
       for (int k = 0; k < ns; ++k) a_fin[k] = act[k] ? 1.0 : 0.0;
       if (cfg.line_search) {
         launch_project(g, 1, 0.0, s);
-        energy(g, P, 0.0, S, S, true, nbufs, s, E0.data());
+        energy(ga, P, 0.0, S, S, true, nbufs, s, E0.data());
         dots(g, dq.p, nbufs.grad.p, nbufs, dd.data(), s);
         for (int k = 0; k < ns; ++k) {
           qdg[k] = dd[3 * k];
@@ -384,12 +455,16 @@ struct Engine {
         }
         int other = 1 - cur;
         int n_ls = n_act;
-        Geo gt = g;
+        Geo gt = g;  // trial positions of the scenes still searching
         gt.alpha_s = sc_alpha.p;
+        gt.sc_act = sc_search.p;
+        int pass = 0, early = 0;  // early: scenes that finished before the last pass
         while (n_ls > 0) {
+          put_mask(sc_search, h_search, ls);
           put_alpha(a_cull);
-          cull(gt, P, 2, 0.0, cs, sets[other], nullptr, nullptr, s);
+          cull_set(gt, 2, sets[other]);
           energy(gt, P, 0.0, sets[other], S, true, nbufs, s, E1.data());
+          ++pass;
           st.bytes_moved += bytes_cull(sets[other]) + 48.0 * nv + 116.0 * (sets[other].npt + sets[other].nee);
           for (int k = 0; k < ns; ++k) {
             if (!ls[k]) continue;
@@ -411,10 +486,21 @@ struct Engine {
               ls[k] = 0;
               --n_ls;
               a_fin[k] = alpha * 2;
+              fin_pass[k] = pass;
             } else {
               a_cull[k] = alpha;
             }
           }
+        }
+        for (int k = 0; k < ns; ++k)
+          if (act[k] && fin_pass[k] < pass) ++early;
+        if (early) {
+          // Adopted set: every iterating scene at the step of its accepted trial (the
+          // trial culls above covered only the scenes still searching).
+          Geo gd = ga;
+          gd.alpha_s = sc_alpha.p;
+          put_alpha(a_cull);
+          cull_set(gd, 2, sets[other]);
         }
         for (int k = 0; k < ns; ++k) {
           st.ls_trials += trials[k];
@@ -648,7 +734,16 @@ int abd_cull(abd_handle* h, int vtn, const double* q, const double* dq, int* cou
     std::vector<double> tp(e.ns, 1.0), tg(e.ns, 1.0);
     abd::Geo g = e.geo();
     abd::PairSet& S = e.sets[e.cur];
-    abd::cull(g, e.P, vtn, 1.0, e.cs, vtn == 3 ? e.sets[2] : S, tp.data(), tg.data(), e.s);
+    if (vtn == 3 && e.cfg.iaabb <= 1) {
+      std::vector<double> tb(e.ns, 1.0);
+      abd::sh_bound(g, e.P, e.sh, S, e.shw, e.cs, tb.data(), e.s);
+      double t = 1.0;
+      for (int k = 0; k < e.ns; ++k) t = std::min(t, tb[k]);
+      if (toi) *toi = t;
+      return (int)ABD_OK;
+    }
+    if (vtn == 3) abd::cull(g, e.P, vtn, 1.0, e.cs, e.sets[2], tp.data(), tg.data(), e.s);
+    else e.cull_set(g, vtn == 1 ? 1 : 2, S);
     CK(cudaStreamSynchronize(e.s));
     if (vtn == 3) {
       double t = 1.0;
@@ -696,7 +791,7 @@ static int newton_system_at(Engine& e, const double* q) {
   CK(cudaMemsetAsync(e.dq.p, 0, n * sizeof(double), e.s));
   abd::Geo g = e.geo();
   abd::launch_project(g, 0, 0.0, e.s);
-  abd::cull(g, e.P, 1, 0.0, e.cs, e.sets[e.cur], nullptr, nullptr, e.s);
+  e.cull_set(g, 1, e.sets[e.cur]);
   abd::assemble(g, e.P, e.sets[e.cur], e.nbufs, e.s);
   CK(cudaStreamSynchronize(e.s));
   e.last_cull_set = e.cur;

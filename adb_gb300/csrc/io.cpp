@@ -243,6 +243,19 @@ extern "C" int abd_create_from_files(const char* config_json, const char* scene_
   c.ee_fric = cfgj.flag("ee_friction", true);
   c.clip = pi ? (int)pi->num("clip", 0) : 0;
   c.pcg_max_iter = (int)cfgj.num("pcg_max_iter", 5000);
+  c.iaabb = (int)cfgj.num("iaabb", 3);
+  c.full_ccd = cfgj.flag("full_ccd", true);
+  c.safe_factor = cfgj.num("safe_factor", 1.0);
+  const JV* sh = cfgj.get("spatial hashing");
+  c.sh_min_xyz = sh ? sh->num("min_xyz", -10.0) : -10.0;
+  c.sh_dx = sh ? sh->num("dx", 0.8) : 0.8;
+  c.sh_xyz_bits = sh ? (int)sh->num("xyz_bits", 6) : 6;
+  c.sh_fix_edge_trajectory = cfgj.flag("sh_fix_edge_trajectory", false);
+  c.dq_tol = pd ? pd->num("dq_tol", 0.0) : 0.0;
+  const JV* dmp = cfgj.get("damping");
+  c.damping = dmp ? dmp->flag("enable", false) : 0;
+  c.damp_alpha = dmp ? dmp->num("alpha", 5e-2) : 5e-2;
+  c.damp_beta = dmp ? dmp->num("beta", 2.5e-2) : 2.5e-2;
 
   std::string dir = scene_json;
   size_t sl = dir.find_last_of('/');

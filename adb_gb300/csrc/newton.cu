@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, i
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   int A = tup[4 * p], a = tup[4 * p + 1], B = tup[4 * p + 2], b = tup[4 * p + 3];
+  if (!scene_on(g, A)) return;  // scene not iterating: its blocks are not used
   int vid[4];
   int na;
   if (kind == 0) {
@@ -200,7 +201,8 @@ __global__ void k_seg(int nov, int n, const int* pov, int* seg) {
 // Per-overlap sums of the pair records: 8 warps, each owns components c = w + 8k;
 // lanes stride over the overlap's pairs; fixed shuffle tree.
 __global__ void __launch_bounds__(256) k_ov_reduce(int nov, const int* pt_seg, const int* ee_seg, const double* ptC,
-                                                   int npt, const double* eeC, int nee, double* ovr, int* has) {
+                                                   int npt, const double* eeC, int nee, double* ovr, int* has,
+                                                   double off_scale) {
   int u = blockIdx.x;
   if (u >= nov) return;
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -212,7 +214,8 @@ __global__ void __launch_bounds__(256) k_ov_reduce(int nov, const int* pt_seg, c
     for (int p = e0 + lane; p < e1; p += 32) s += eeC[(size_t)c * nee + p];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) ovr[(size_t)u * CONTRIB + c] = s;
+    // the off-diagonal block takes the damping scale (1 + beta), like every matrix entry
+    if (lane == 0) ovr[(size_t)u * CONTRIB + c] = (c >= 288 && c < 432) ? s * off_scale : s;
   }
 }
 
@@ -233,10 +236,17 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
   const double* q = g.q + 12 * b;
   double dt = P.dt;
   double val = 0.0;
-  if (m < 0.0) {
-    // static body: identity block, zero gradient (mutils.cpp:55-56, 70)
-    if (is_h) D[144 * b + t] = (i == j) ? 1.0 : 0.0;
-    else grad[12 * b + i] = 0.0;
+  if (m < 0.0 || !scene_on(g, b)) {
+    // static body: identity block, zero gradient (mutils.cpp:55-56, 70); bodies of scenes
+    // that are not iterating get the same (their step is zero)
+    if (is_h) {
+      double v = (i == j) ? 1.0 : 0.0;
+      // damping_sparse scales every body's block (mutils.cpp:106-115)
+      if (P.damp) v = v * (1 + P.damp_beta) + ((i == j) ? (i < 3 ? m : g.Ic[b]) * (P.damp_alpha - P.damp_beta) : 0.0);
+      D[144 * b + t] = v;
+    } else {
+      grad[12 * b + i] = 0.0;
+    }
     if (t == 0)
       for (int kk = vg_seg[b]; kk < vg_seg[b + 1]; ++kk) {
         int v = g.v_off[b] + vg[2 * kk + 1];
@@ -318,8 +328,13 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
     if (is_h) val += rec[(isI ? 0 : 144) + t];
     else val += rec[(isI ? 432 : 444) + i];
   }
-  if (is_h) D[144 * b + t] = val;
-  else grad[12 * b + i] = val;
+  if (is_h) {
+    // damping_sparse (mutils.cpp:106-115): H (1 + beta) + diag(m, Ic) (alpha - beta)
+    if (P.damp) val = val * (1 + P.damp_beta) + ((i == j) ? mi * (P.damp_alpha - P.damp_beta) : 0.0);
+    D[144 * b + t] = val;
+  } else {
+    grad[12 * b + i] = val;
+  }
 }
 
 // Inverse of each SPD diagonal block via Cholesky (block-Jacobi preconditioner).
@@ -832,6 +847,10 @@ __global__ void __launch_bounds__(256) k_energy(Geo g, Params P, EnergyArgs a) {
     }
     const int s = lo;
     const int S1 = a.ns + 1;
+    if (g.sc_act && !g.sc_act[s]) {  // scene not processed: its total is not used
+      if (threadIdx.x == 0) a.partial[c] = 0.0;
+      continue;
+    }
     int len[1 + NSEG], beg[1 + NSEG];
     len[0] = a.with_bi ? g.sc_end[s] - g.sc_beg[s] : 0;
     beg[0] = g.sc_beg[s];
@@ -897,6 +916,41 @@ __global__ void __launch_bounds__(256) k_scene_dots(const int* sc_beg, const int
   }
 }
 
+// Per scene: a.b, |b|^2, |a - b|^2 (same layout and order as k_scene_dots).
+__global__ void __launch_bounds__(256) k_scene_diff(const int* sc_beg, const int* sc_end, const double* a,
+                                                   const double* b, double* out) {
+  __shared__ double sh[80];
+  int s = blockIdx.x;
+  double s0 = 0, s1 = 0, s2 = 0;
+  for (int k = sc_beg[s] + (int)threadIdx.x; k < sc_end[s]; k += blockDim.x) {
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (int i = 12 * k; i < 12 * k + 12; ++i) {
+      double d = a[i] - b[i];
+      t0 += a[i] * b[i];
+      t1 += b[i] * b[i];
+      t2 += d * d;
+    }
+    s0 += t0;
+    s1 += t1;
+    s2 += t2;
+  }
+  block_sum2(s0, s1, sh);
+  __syncthreads();
+  double d = 0;
+  block_sum2(s2, d, sh);
+  if (threadIdx.x == 0) {
+    out[3 * s] = s0;
+    out[3 * s + 1] = s1;
+    out[3 * s + 2] = s2;
+  }
+}
+
+// dst = src on the bodies of scenes with on[scene] != 0
+__global__ void k_copy_scene(double* dst, const double* src, int n, const int* bscene, const int* on) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && on[bscene[i / 12]]) dst[i] = src[i];
+}
+
 // v *= f[scene of body]
 __global__ void k_scale_scene(double* v, int n, const int* bscene, const double* f) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -948,7 +1002,8 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
   if (nov) {
     KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, npt, S.pt_ov.p, B.pt_seg.p));
     KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, nee, S.ee_ov.p, B.ee_seg.p));
-    KLAUNCH(K_OV_REDUCE, s, k_ov_reduce<<<nov, 256, 0, s>>>(nov, B.pt_seg.p, B.ee_seg.p, B.pt_c.p, npt, B.ee_c.p, nee, B.ovr.p, B.has.p));
+    KLAUNCH(K_OV_REDUCE, s, k_ov_reduce<<<nov, 256, 0, s>>>(nov, B.pt_seg.p, B.ee_seg.p, B.pt_c.p, npt, B.ee_c.p, nee, B.ovr.p, B.has.p,
+                                                                P.damp ? 1 + P.damp_beta : 1.0));
   }
   KLAUNCH(K_BODY_SYSTEM, s, k_body_system<<<nb, 160, 0, s>>>(g, P, S.row_ptr.p, S.col.p, S.upidx.p, B.ovr.p, B.has.p, S.vg.p, S.vg_seg.p,
                                    S.vg_lam.p, B.D.p, B.grad.p));
@@ -1077,6 +1132,19 @@ void dots(const Geo& g, const double* dq, const double* grad, NewtonBufs& B, dou
   KLAUNCH(K_DOTS, s, k_scene_dots<<<g.ns, 256, 0, s>>>(g.sc_beg, g.sc_end, dq, grad, B.e_out.p));
   CK(cudaMemcpyAsync(out, B.e_out.p, 3 * (size_t)g.ns * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+}
+
+void scene_diff(const Geo& g, const double* a, const double* b, NewtonBufs& B, double* out, cudaStream_t s) {
+  B.e_out.ensure(3 * (size_t)g.ns);
+  KLAUNCH(K_DOTS, s, k_scene_diff<<<g.ns, 256, 0, s>>>(g.sc_beg, g.sc_end, a, b, B.e_out.p));
+  CK(cudaMemcpyAsync(out, B.e_out.p, 3 * (size_t)g.ns * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+}
+
+void launch_copy_scene(const Geo& g, double* dst, const double* src, const int* on, cudaStream_t st) {
+  int n = 12 * g.nb;
+  if (n <= 0) return;
+  KLAUNCH(K_VEC, st, k_copy_scene<<<nblk(n, 256), 256, 0, st>>>(dst, src, n, g.bscene, on));
 }
 
 void launch_scale_scene(const Geo& g, double* v, const double* f, cudaStream_t st) {

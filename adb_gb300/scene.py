@@ -57,7 +57,18 @@ class Config:
     pt_friction: bool = True
     ee_friction: bool = True
     clip: int = 0                  # params_int.clip
-    iaabb: int = 3
+    iaabb: int = 3                 # odd: iAABB culling; even: spatial hash; > 1: iAABB step bound
+    full_ccd: bool = True          # spatial-hash step bound: hashed trajectories (else the d_sqrt bound)
+    safe_factor: float = 1.0       # spatial-hash distance scale
+    sh_min_xyz: float = -10.0      # "spatial hashing": min_xyz, dx, xyz_bits, n_buffer
+    sh_dx: float = 0.8
+    sh_bits: int = 6
+    sh_n_buffer: int = 512
+    sh_fix_edge_trajectory: bool = False   # register edge trajectories by both ends (reference: start only)
+    damping: bool = False          # "damping": {"enable", "alpha", "beta"} (mutils.cpp:106-115)
+    damp_alpha: float = 5e-2
+    damp_beta: float = 2.5e-2
+    solver: str = "sparse"         # "solver": the reference's factorization choice; one PCG here
     # GPU solver controls (no reference counterpart: the reference factorizes directly)
     pcg_rel_tol: float = 1e-14
     pcg_max_iter: int = 5000
@@ -104,6 +115,19 @@ def load_config(path: str) -> Config:
     c.ee_friction = bool(d.get("ee_friction", c.ee_friction))
     c.clip = int(pi.get("clip", c.clip))
     c.iaabb = int(d.get("iaabb", c.iaabb))
+    c.full_ccd = bool(d.get("full_ccd", c.full_ccd))
+    c.safe_factor = float(d.get("safe_factor", c.safe_factor))
+    sh = d.get("spatial hashing", {})
+    c.sh_min_xyz = float(sh.get("min_xyz", c.sh_min_xyz))
+    c.sh_dx = float(sh.get("dx", c.sh_dx))
+    c.sh_bits = int(sh.get("xyz_bits", c.sh_bits))
+    c.sh_n_buffer = int(sh.get("n_buffer", c.sh_n_buffer))
+    c.sh_fix_edge_trajectory = bool(d.get("sh_fix_edge_trajectory", c.sh_fix_edge_trajectory))
+    dmp = d.get("damping", {})
+    c.damping = bool(dmp.get("enable", c.damping))
+    c.damp_alpha = float(dmp.get("alpha", c.damp_alpha))
+    c.damp_beta = float(dmp.get("beta", c.damp_beta))
+    c.solver = str(d.get("solver", c.solver))
     c.pcg_rel_tol = float(d.get("pcg_rel_tol", c.pcg_rel_tol))
     c.pcg_max_iter = int(d.get("pcg_max_iter", c.pcg_max_iter))
     return c
@@ -115,9 +139,13 @@ def config_to_json(c: Config) -> dict:
         "dt": c.dt, "max_iter": c.max_iter, "gravity": c.gravity, "line_search": c.line_search,
         "col_set": True, "ee": c.ee, "pt": c.pt, "ground": c.ground, "uppper_bound": c.upper_bound,
         "mu": c.mu, "backoff": c.backoff, "eps_x": c.eps_x, "psd": c.psd, "iaabb": c.iaabb,
+        "full_ccd": c.full_ccd, "safe_factor": c.safe_factor,
+        "spatial hashing": {"min_xyz": c.sh_min_xyz, "max_xyz": -c.sh_min_xyz, "dx": c.sh_dx,
+                            "n_buffer": c.sh_n_buffer, "xyz_bits": c.sh_bits, "set_size": 1},
+        "sh_fix_edge_trajectory": c.sh_fix_edge_trajectory,
         "evh": c.evh, "vg_friction": c.vg_friction, "pt_friction": c.pt_friction,
-        "ee_friction": c.ee_friction, "kappa": c.kappa, "solver": "sparse",
-        "damping": {"enable": False, "alpha": 5e-2, "beta": 2.5e-2},
+        "ee_friction": c.ee_friction, "kappa": c.kappa, "solver": c.solver,
+        "damping": {"enable": c.damping, "alpha": c.damp_alpha, "beta": c.damp_beta},
         "params_double": {"tol": c.tol, "c1": c.c1, "max_uk": c.max_uk, "dq_tol": c.dq_tol},
         "params_int": {"clip": c.clip, "thres": 100},
         "dhat": c.dhat, "ortho_kappa": c.ortho_kappa, "ground_y": -c.ground_offset,

@@ -31,7 +31,8 @@ typedef enum {
   ABD_ERR_PCG_NOCONV = 6,     /* PCG hit its iteration cap (the step is still taken) */
   ABD_ERR_CUDA = 7,           /* CUDA runtime error; see abd_last_error */
   ABD_ERR_INVALID = 8,        /* invalid argument */
-  ABD_ERR_IO = 9              /* config / scene / mesh file could not be read */
+  ABD_ERR_IO = 9,             /* config / scene / mesh file could not be read */
+  ABD_ERR_SAME_DIRECTION = 10 /* Newton step repeats the previous one (abd.cpp:181-188) */
 } abd_status;
 
 /* Step parameters. Field names follow the reference's config.json keys
@@ -57,6 +58,19 @@ typedef struct {
   int ground, pt, ee, psd, line_search, upper_bound;
   int vg_fric, pt_fric, ee_fric, clip;
   int pcg_max_iter;
+  /* broad-phase selection (view/control.cpp:37-68): iaabb odd culls with iAABB, even with
+   * the spatial hash; iaabb > 1 bounds the step with the iAABB trajectory pass, otherwise
+   * with step_size_upper_bound (hashed trajectories when full_ccd, else the d_sqrt bound) */
+  int iaabb, full_ccd;
+  double safe_factor;    /* spatial-hash distance scale */
+  double sh_min_xyz, sh_dx; /* "spatial hashing": cell = int(max(x - min_xyz, 0) / dx) */
+  int sh_xyz_bits;       /* bucket = low xyz_bits bits of each cell coordinate */
+  int sh_fix_edge_trajectory; /* 1: register edge trajectories by both ends (the reference
+                                 registers them by their start, upper_bound.cpp:151) */
+  double dq_tol;         /* params_double.dq_tol: same-direction stop (abd.cpp:181-188) */
+  int damping;           /* "damping": {"enable"}: H (1 + beta) + diag(m, Ic) (alpha - beta)
+                            (damping_sparse, mutils.cpp:106-115) */
+  double damp_alpha, damp_beta;
 } abd_config;
 
 /* Scene: bodies with their rest meshes (local vertex ids per body). */

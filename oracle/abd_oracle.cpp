@@ -33,6 +33,13 @@ struct Config {
       gravity_y, ls_grad_tol;
   // ints
   int max_iter, ground, pt, ee, psd, line_search, upper_bound, vg_fric, pt_fric, ee_fric, clip, n_threads;
+  // broad-phase selection and spatial hashing ("iaabb", "full_ccd", "safe_factor",
+  // "spatial hashing" {min_xyz, dx, xyz_bits}; view/control.cpp:37-68)
+  double safe_factor, sh_min_xyz, sh_dx;
+  int iaabb, full_ccd, sh_bits, sh_fix_edge;
+  // "damping": {enable, alpha, beta} (view/control.cpp:35, 60-61)
+  int damp;
+  double damp_alpha, damp_beta;
 };
 
 struct I4 {
@@ -67,7 +74,7 @@ struct Stats {
   double toi_min, alpha_min, t_ipc, t_solver, t_ccd, t_ls;
 };
 
-enum { ST_OK = 0, ST_NAN = 1, ST_LS_STALL = 2, ST_TOI_TINY = 4, ST_NOT_SPD = 5 };
+enum { ST_OK = 0, ST_NAN = 1, ST_LS_STALL = 2, ST_TOI_TINY = 4, ST_NOT_SPD = 5, ST_SAME_DIR = 10 };
 
 struct Scene {
   Config cfg;
@@ -83,6 +90,7 @@ struct Scene {
   std::vector<V3> X0;        // positions at q0
   int iter = 0;              // cumulative Newton counter (abd.h:53, never reset per frame)
   int g_cnt = 0, p_cnt = 0;  // consecutive tiny-TOI counters (iaabb.cpp:302-313, 533-540)
+  std::vector<double> lastdq;  // previous Newton step, kept across frames (abd.h member)
   PairSet set;
   std::vector<Mat<2, 12>> pt_tk, ee_tk;
   std::vector<double> pt_lam, ee_lam, g_lam;
@@ -381,6 +389,291 @@ static double iaabb(Scene& s, int vtn, PairSet* out) {
   P.pt_off[nov] = (int)P.pt.size();
   P.ee_off[nov] = (int)P.ee.size();
   P.vg = vg;
+  return 1.0;
+}
+
+// ---------------------------------------------------------------------------------
+// Spatial-hash broad phase (iaabb even): spatial_hashing.cpp:11-211 and the global-list
+// branches of gen_collision_set (col_set.cpp:20-339) and step_size_upper_bound
+// (upper_bound.cpp:16-277). Cells are tovec3i(x) = int(max(x - min_xyz, 0) / dx) per
+// axis; a cell's bucket keeps the low xyz_bits bits of each axis (hash(), :11-21), so
+// cells that agree modulo 2^bits share a bucket. Buckets here are unbounded (the
+// reference keeps n_buffer entries per bucket and logs an error beyond that).
+struct SHash {
+  int bits;
+  double min_xyz, dx;
+  std::vector<std::vector<int>> bucket;  // entries: (body << 16) | pid, as Primitive::as_uint
+  SHash(int b, double mn, double d) : bits(b), min_xyz(mn), dx(d), bucket(size_t(1) << (3 * b)) {}
+  int cell(double f) const { return (int)(std::max(f - min_xyz, 0.0) / dx); }
+  int hash(int i, int j, int k) const {
+    int m = (1 << bits) - 1;
+    return (((i & m) << bits | (j & m)) << bits) | (k & m);
+  }
+  void reg(const V3& lo, const V3& hi, int body, int pid) {
+    int l[3] = {cell(lo.x), cell(lo.y), cell(lo.z)}, u[3] = {cell(hi.x), cell(hi.y), cell(hi.z)};
+    for (int i = l[0]; i <= u[0]; ++i)
+      for (int j = l[1]; j <= u[1]; ++j)
+        for (int k = l[2]; k <= u[2]; ++k) bucket[hash(i, j, k)].push_back((body << 16) | pid);
+  }
+  // query_interval (:71-113): entries of every bucket the cell range touches, other
+  // bodies only, sorted and unique.
+  void query(const V3& lo, const V3& hi, int body_exl, std::vector<int>& out) const {
+    out.clear();
+    int l[3] = {cell(lo.x), cell(lo.y), cell(lo.z)}, u[3] = {cell(hi.x), cell(hi.y), cell(hi.z)};
+    for (int i = l[0]; i <= u[0]; ++i)
+      for (int j = l[1]; j <= u[1]; ++j)
+        for (int k = l[2]; k <= u[2]; ++k)
+          for (int e : bucket[hash(i, j, k)])
+            if ((e >> 16) != body_exl) out.push_back(e);
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+  }
+};
+
+static inline V3 vadd(const V3& a, double d) { return V3(a.x + d, a.y + d, a.z + d); }
+
+// Orders a pair set the way the overlap-based paths store it: overlaps (I < J) sorted,
+// and per overlap the PT pairs with the vertex on I, then on J, then the EE pairs, each
+// by (primitive of the first body, primitive of the second). The reference's spatial-hash
+// path appends the pairs of its OpenMP threads in scheduling order, so only the set is
+// defined there.
+static void canonical_set(const std::vector<I4>& pt, const std::vector<int8_t>& ptt, const std::vector<I4>& ee,
+                          const std::vector<int8_t>& eet, PairSet& P) {
+  struct K {
+    long long key;
+    int src;
+  };
+  auto pt_key = [](const I4& p) {
+    int A = p[0], B = p[2];
+    long long lo = std::min(A, B), hi = std::max(A, B), sub = A < B ? 0 : 1;
+    return (lo << 47) | (hi << 32) | (sub << 30) | ((long long)p[1] << 15) | (long long)p[3];
+  };
+  auto ee_key = [](const I4& p) {
+    return ((long long)p[0] << 47) | ((long long)p[2] << 32) | (2ll << 30) | ((long long)p[1] << 15) | (long long)p[3];
+  };
+  std::vector<K> kp(pt.size()), ke(ee.size());
+  for (size_t k = 0; k < pt.size(); ++k) kp[k] = K{pt_key(pt[k]), (int)k};
+  for (size_t k = 0; k < ee.size(); ++k) ke[k] = K{ee_key(ee[k]), (int)k};
+  auto cmp = [](const K& a, const K& b) { return a.key < b.key; };
+  std::sort(kp.begin(), kp.end(), cmp);
+  std::sort(ke.begin(), ke.end(), cmp);
+  std::vector<long long> bp;
+  for (auto& k : kp) bp.push_back(k.key >> 32);
+  for (auto& k : ke) bp.push_back(k.key >> 32);
+  std::sort(bp.begin(), bp.end());
+  bp.erase(std::unique(bp.begin(), bp.end()), bp.end());
+  int nov = (int)bp.size();
+  P.ov.assign(nov, Overlap{});
+  for (int o = 0; o < nov; ++o) {
+    P.ov[o].I = (int)(bp[o] >> 15);
+    P.ov[o].J = (int)(bp[o] & 0x7fff);
+  }
+  P.pt.clear(); P.ee.clear(); P.pt_ty.clear(); P.ee_ty.clear();
+  P.pt_off.assign(nov + 1, 0);
+  P.ee_off.assign(nov + 1, 0);
+  size_t a = 0, b = 0;
+  for (int o = 0; o < nov; ++o) {
+    P.pt_off[o] = (int)P.pt.size();
+    P.ee_off[o] = (int)P.ee.size();
+    for (; a < kp.size() && (kp[a].key >> 32) == bp[o]; ++a) {
+      P.pt.push_back(pt[kp[a].src]);
+      P.pt_ty.push_back(ptt[kp[a].src]);
+    }
+    for (; b < ke.size() && (ke[b].key >> 32) == bp[o]; ++b) {
+      P.ee.push_back(ee[ke[b].src]);
+      P.ee_ty.push_back(eet[ke[b].src]);
+    }
+  }
+  P.pt_off[nov] = (int)P.pt.size();
+  P.ee_off[nov] = (int)P.ee.size();
+}
+
+// gen_collision_set (col_set.cpp:20-339), global point / edge / triangle lists.
+static void sh_collision_set(Scene& s, bool vt2, PairSet* out) {
+  project_all(s, vt2 ? 2 : 1);
+  const double sf = s.cfg.safe_factor;
+  const double thr = s.bp.dhat * (sf * sf);
+  const double qd = s.d_sqrt * sf;
+  int nb = (int)s.b.size();
+  std::vector<std::array<int, 2>> vg;
+  if (s.cfg.ground)
+    for (int I = 0; I < nb; ++I)
+      for (int v = 0; v < s.b[I].nv; ++v) {
+        double d = Xat(s, I, v).y + s.cfg.ground_offset;
+        d = d * d;
+        if (d < thr) vg.push_back({I, v});
+      }
+  std::vector<I4> pt, ee;
+  std::vector<int8_t> ptt, eet;
+  std::vector<int> cand;
+  if (s.cfg.pt) {
+    SHash h(s.cfg.sh_bits, s.cfg.sh_min_xyz, s.cfg.sh_dx);
+    for (int I = 0; I < nb; ++I)
+      for (int v = 0; v < s.b[I].nv; ++v) {
+        V3 p = Xat(s, I, v);
+        h.reg(p, p, I, v);
+      }
+    for (int J = 0; J < nb; ++J)
+      for (int f = 0; f < s.b[J].nf; ++f) {
+        V3 t[3];
+        face_at(s, s.X, J, f, t);
+        V3 lo = vmin(vmin(t[0], t[1]), t[2]), hi = vmax(vmax(t[0], t[1]), t[2]);
+        h.query(vadd(lo, -qd), vadd(hi, qd), J, cand);
+        for (int e : cand) {
+          int I = e >> 16, v = e & 0xffff;
+          V3 p = Xat(s, I, v);
+          PTType ty = pt_type(p, t[0], t[1], t[2]);
+          double d = pt_dist(p, t[0], t[1], t[2], ty);
+          if (d < thr) {
+            pt.push_back(I4{{I, v, J, f}});
+            ptt.push_back((int8_t)ty);
+          }
+        }
+      }
+  }
+  if (s.cfg.ee) {
+    SHash h(s.cfg.sh_bits, s.cfg.sh_min_xyz, s.cfg.sh_dx);
+    for (int I = 0; I < nb; ++I)
+      for (int e = 0; e < s.b[I].ne; ++e) {
+        V3 a[2];
+        edge_at(s, s.X, I, e, a);
+        h.reg(vmin(a[0], a[1]), vmax(a[0], a[1]), I, e);
+      }
+    for (int J = 0; J < nb; ++J)
+      for (int ej = 0; ej < s.b[J].ne; ++ej) {
+        V3 b2[2];
+        edge_at(s, s.X, J, ej, b2);
+        h.query(vadd(vmin(b2[0], b2[1]), -qd), vadd(vmax(b2[0], b2[1]), qd), J, cand);
+        for (int e : cand) {
+          int I = e >> 16, ei = e & 0xffff;
+          if (I > J) continue;
+          V3 a[2];
+          edge_at(s, s.X, I, ei, a);
+          EEType ty = ee_type(a[0], a[1], b2[0], b2[1]);
+          double d = ee_dist(a[0], a[1], b2[0], b2[1], ty);
+          if (d < thr) {
+            ee.push_back(I4{{I, ei, J, ej}});
+            eet.push_back((int8_t)ty);
+          }
+        }
+      }
+  }
+  canonical_set(pt, ptt, ee, eet, *out);
+  out->vg = vg;
+}
+
+// step_size_upper_bound (upper_bound.cpp:16-277). With full_ccd the trajectories are
+// hashed (vertex trajectories as segments; edge trajectories, as in the reference,
+// registered by their start position only unless sh_fix_edge is set) and every candidate
+// that shares a bucket gets an exact time of impact; otherwise the bound is
+// d_sqrt / 2 / max_I |dq_I|_1 * safe_factor, lowered by the TOIs of the current pairs.
+static double sh_upper_bound(Scene& s) {
+  int nb = (int)s.b.size();
+  project_all(s, 2);
+  for (int I = 0; I < nb; ++I) {
+    Body& c = s.b[I];
+    for (int v = 0; v < c.nv; ++v) s.Xq[c.v_off + v] = project_pt(c.q, &s.rest[3 * (c.v_off + v)]);
+  }
+  auto ground_t = [&](int I, int v) {
+    double d2 = Xat(s, I, v).y + s.cfg.ground_offset;
+    if (!(d2 < 0)) return 1.0;
+    double d1 = Xqat(s, I, v).y + s.cfg.ground_offset;
+    return d1 / (d1 - d2);
+  };
+  double toi = 1.0;
+  std::vector<int> cand;
+  if (s.cfg.full_ccd) {
+    if (s.cfg.ground)
+      for (int I = 0; I < nb; ++I)
+        for (int v = 0; v < s.b[I].nv; ++v) toi = std::min(toi, ground_t(I, v));
+    if (s.cfg.pt) {
+      SHash h(s.cfg.sh_bits, s.cfg.sh_min_xyz, s.cfg.sh_dx);
+      for (int I = 0; I < nb; ++I)
+        for (int v = 0; v < s.b[I].nv; ++v) {
+          V3 p0 = Xqat(s, I, v), p1 = Xat(s, I, v);
+          h.reg(vmin(p0, p1), vmax(p0, p1), I, v);
+        }
+      for (int J = 0; J < nb; ++J)
+        for (int f = 0; f < s.b[J].nf; ++f) {
+          V3 f0[3], f1[3];
+          face_at(s, s.Xq, J, f, f0);
+          face_at(s, s.X, J, f, f1);
+          V3 lo = vmin(vmin(vmin(f0[0], f0[1]), f0[2]), vmin(vmin(f1[0], f1[1]), f1[2]));
+          V3 hi = vmax(vmax(vmax(f0[0], f0[1]), f0[2]), vmax(vmax(f1[0], f1[1]), f1[2]));
+          h.query(lo, hi, J, cand);
+          for (int e : cand) {
+            int I = e >> 16, v = e & 0xffff;
+            toi = std::min(toi, pt_collision_time(Xqat(s, I, v), f0, Xat(s, I, v), f1));
+          }
+        }
+    }
+    if (s.cfg.ee) {
+      SHash h(s.cfg.sh_bits, s.cfg.sh_min_xyz, s.cfg.sh_dx);
+      for (int I = 0; I < nb; ++I)
+        for (int e = 0; e < s.b[I].ne; ++e) {
+          V3 a0[2], a1[2];
+          edge_at(s, s.Xq, I, e, a0);
+          edge_at(s, s.X, I, e, a1);
+          V3 lo = vmin(a0[0], a0[1]), hi = vmax(a0[0], a0[1]);
+          if (s.cfg.sh_fix_edge) {
+            lo = vmin(lo, vmin(a1[0], a1[1]));
+            hi = vmax(hi, vmax(a1[0], a1[1]));
+          }
+          h.reg(lo, hi, I, e);
+        }
+      for (int J = 0; J < nb; ++J)
+        for (int ej = 0; ej < s.b[J].ne; ++ej) {
+          V3 b0[2], b1[2];
+          edge_at(s, s.Xq, J, ej, b0);
+          edge_at(s, s.X, J, ej, b1);
+          V3 lo = vmin(vmin(b0[0], b0[1]), vmin(b1[0], b1[1])), hi = vmax(vmax(b0[0], b0[1]), vmax(b1[0], b1[1]));
+          h.query(lo, hi, J, cand);
+          for (int e : cand) {
+            int I = e >> 16, ei = e & 0xffff;
+            if (I > J) continue;
+            V3 a0[2], a1[2];
+            edge_at(s, s.Xq, I, ei, a0);
+            edge_at(s, s.X, I, ei, a1);
+            toi = std::min(toi, ee_collision_time(a0, b0, a1, b1));
+          }
+        }
+    }
+    return toi;
+  }
+  double n1 = 0.0;
+  for (int I = 0; I < nb; ++I) {
+    double a = 0.0;
+    for (int i = 0; i < 12; ++i) a += std::fabs(s.b[I].dq[i]);
+    n1 = std::max(n1, a);
+  }
+  toi = s.d_sqrt / 2.0 / n1 * s.cfg.safe_factor;
+  toi = std::min(1.0, toi);
+  const PairSet& P = s.set;
+  for (auto& v : P.vg) toi = std::min(toi, ground_t(v[0], v[1]));
+  for (auto& p : P.pt) {
+    V3 f0[3], f1[3];
+    face_at(s, s.Xq, p[2], p[3], f0);
+    face_at(s, s.X, p[2], p[3], f1);
+    toi = std::min(toi, pt_collision_time(Xqat(s, p[0], p[1]), f0, Xat(s, p[0], p[1]), f1));
+  }
+  for (auto& p : P.ee) {
+    V3 a0[2], a1[2], b0[2], b1[2];
+    edge_at(s, s.Xq, p[0], p[1], a0);
+    edge_at(s, s.X, p[0], p[1], a1);
+    edge_at(s, s.Xq, p[2], p[3], b0);
+    edge_at(s, s.X, p[2], p[3], b1);
+    toi = std::min(toi, ee_collision_time(a0, b0, a1, b1));
+  }
+  return toi;
+}
+
+// Culling dispatch (abd.cpp:48-51, 157-174; line_search.cpp:88-110): iaabb odd culls with
+// the iAABB brute force, even with the spatial hash; iaabb > 1 bounds the step with the
+// iAABB trajectory pass, otherwise with step_size_upper_bound.
+static double cull(Scene& s, int vtn, PairSet* out) {
+  if (vtn == 3) return s.cfg.iaabb > 1 ? iaabb(s, 3, nullptr) : sh_upper_bound(s);
+  if (s.cfg.iaabb % 2) return iaabb(s, vtn, out);
+  sh_collision_set(s, vtn == 2, out);
   return 1.0;
 }
 
@@ -718,6 +1011,17 @@ static void assemble(Scene& s, BlockSys& sys) {
   }
   for (int I = 0; I < nb; ++I)
     for (int k = 0; k < 144; ++k) sys.diag[I].a[k] += s.b[I].hess.a[k];
+  if (s.cfg.damp) {
+    // damping_sparse (mutils.cpp:106-115): every entry scaled by 1 + beta, then
+    // mass (translation) or Ic (the rest) times alpha - beta on the diagonal
+    double sc = 1 + s.cfg.damp_beta, dab = s.cfg.damp_alpha - s.cfg.damp_beta;
+    for (int I = 0; I < nb; ++I) {
+      for (int k = 0; k < 144; ++k) sys.diag[I].a[k] *= sc;
+      for (int j = 0; j < 12; ++j) sys.diag[I].a[13 * j] += (j < 3 ? s.b[I].mass : s.b[I].Ic) * dab;
+    }
+    for (auto& kv : sys.off)
+      for (int k = 0; k < 144; ++k) kv.second.a[k] *= sc;
+  }
 }
 
 // ---------------------------------------------------------------------------------
@@ -1005,7 +1309,7 @@ static double line_search(Scene& s, const std::vector<double>& dq, const std::ve
     for (int i = 0; i < n; ++i) dqk[i] = dq[i] * alpha;
     for (int I = 0; I < (int)s.b.size(); ++I)
       for (int i = 0; i < 12; ++i) s.b[I].dq[i] = dqk[12 * I + i];
-    iaabb(s, 2, &Pn);
+    cull(s, 2, &Pn);
     double E3 = E_barrier_plus_inert(s, Pn, dqk);
     double ef = E_fric(s, dqk);
     double E1 = E3 + ef;
@@ -1035,8 +1339,7 @@ static int implicit_euler(Scene& s) {
   st.alpha_min = 1.0;
   for (auto& c : s.b) std::memcpy(c.q, c.q0, sizeof(c.q));
   for (auto& c : s.b) std::memset(c.dq, 0, sizeof(c.dq));
-  iaabb(s, 1, &s.set);
-  std::vector<double> lastdq;
+  cull(s, 1, &s.set);
   bool term;
   do {
     double t0 = now_s();
@@ -1061,11 +1364,23 @@ static int implicit_euler(Scene& s) {
     double sup_dq = std::sqrt(nrm);
     for (int I = 0; I < nb; ++I)
       for (int i = 0; i < 12; ++i) s.b[I].dq[i] = dq[12 * I + i];
-    if (s.cfg.upper_bound) toi = iaabb(s, 3, nullptr);
+    if (s.cfg.upper_bound) toi = cull(s, 3, nullptr);
     if ((s.cfg.ground && s.g_cnt > 1) || s.p_cnt > 1) return st.status = ST_TOI_TINY;
     if (toi < 1.0) factor = s.cfg.backoff;
     st.toi_min = std::min(st.toi_min, toi);
-    lastdq = dq;
+    // same-direction stop (abd.cpp:180-190); with dq_tol = 0 it can never trigger
+    if (s.iter && s.lastdq.size() == dq.size()) {
+      double dl = 0, ll = 0, df = 0;
+      for (int i = 0; i < 12 * nb; ++i) {
+        dl += dq[i] * s.lastdq[i];
+        ll += s.lastdq[i] * s.lastdq[i];
+        df += (dq[i] - s.lastdq[i]) * (dq[i] - s.lastdq[i]);
+      }
+      double c = dl / (std::sqrt(nrm) * std::sqrt(ll));
+      if (std::fabs(c) > 1.0 - s.cfg.dq_tol && std::sqrt(df) / std::sqrt(nrm) < s.cfg.dq_tol)
+        return st.status = ST_SAME_DIR;
+    }
+    s.lastdq = dq;
     for (auto& v : dq) v *= factor * toi;
     double t3 = now_s();
     // line search (abd.cpp:198-227)
@@ -1201,7 +1516,7 @@ double orc_cull(void* h, int vtn, const double* q, const double* dq, int* counts
     if (dq) std::memcpy(s.b[I].dq, dq + 12 * I, 12 * sizeof(double));
     else std::memset(s.b[I].dq, 0, 12 * sizeof(double));
   }
-  double t = iaabb(s, vtn, vtn == 3 ? nullptr : &s.set);
+  double t = cull(s, vtn, vtn == 3 ? nullptr : &s.set);
   if (counts) {
     counts[0] = (int)s.set.pt.size();
     counts[1] = (int)s.set.ee.size();
@@ -1237,7 +1552,7 @@ int orc_newton_system(void* h, const double* q, double* grad, double* diag, int*
     std::memcpy(s.b[I].q, q + 12 * I, 12 * sizeof(double));
     std::memset(s.b[I].dq, 0, 12 * sizeof(double));
   }
-  iaabb(s, 1, &s.set);
+  cull(s, 1, &s.set);
   BlockSys sys;
   assemble(s, sys);
   int nb = (int)s.b.size();
@@ -1265,7 +1580,7 @@ int orc_newton_dq(void* h, const double* q, double* dq) {
     std::memcpy(s.b[I].q, q + 12 * I, 12 * sizeof(double));
     std::memset(s.b[I].dq, 0, 12 * sizeof(double));
   }
-  iaabb(s, 1, &s.set);
+  cull(s, 1, &s.set);
   BlockSys sys;
   assemble(s, sys);
   std::vector<double> x;
@@ -1281,7 +1596,7 @@ double orc_energy(void* h, const double* q) {
     std::memcpy(s.b[I].q, q + 12 * I, 12 * sizeof(double));
     std::memset(s.b[I].dq, 0, 12 * sizeof(double));
   }
-  iaabb(s, 1, &s.set);
+  cull(s, 1, &s.set);
   std::vector<double> zero(12 * s.b.size(), 0.0);
   return E_barrier_plus_inert(s, s.set, zero);
 }

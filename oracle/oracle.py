@@ -25,7 +25,9 @@ class OracleConfig(C.Structure):
         "dt", "kappa", "dhat", "ortho_kappa", "ground_offset", "mu", "evh", "eps_x", "backoff", "c1", "tol",
         "max_uk", "dq_tol", "gravity_y", "ls_grad_tol")] + [(n, C.c_int) for n in (
             "max_iter", "ground", "pt", "ee", "psd", "line_search", "upper_bound", "vg_fric", "pt_fric",
-            "ee_fric", "clip", "n_threads")]
+            "ee_fric", "clip", "n_threads")] + [(n, C.c_double) for n in ("safe_factor", "sh_min_xyz", "sh_dx")] + [
+        (n, C.c_int) for n in ("iaabb", "full_ccd", "sh_bits", "sh_fix_edge", "damp")] + [
+        (n, C.c_double) for n in ("damp_alpha", "damp_beta")]
 
 
 class OracleStats(C.Structure):
@@ -110,6 +112,10 @@ def make_config(cfg, n_threads: int = 0) -> OracleConfig:
     c.line_search, c.upper_bound = int(cfg.line_search), int(cfg.upper_bound)
     c.vg_fric, c.pt_fric, c.ee_fric = int(cfg.vg_friction), int(cfg.pt_friction), int(cfg.ee_friction)
     c.clip, c.n_threads = int(cfg.clip), int(n_threads)
+    c.safe_factor, c.sh_min_xyz, c.sh_dx = cfg.safe_factor, cfg.sh_min_xyz, cfg.sh_dx
+    c.iaabb, c.full_ccd, c.sh_bits, c.sh_fix_edge = int(cfg.iaabb), int(cfg.full_ccd), int(cfg.sh_bits), int(
+        cfg.sh_fix_edge_trajectory)
+    c.damp, c.damp_alpha, c.damp_beta = int(cfg.damping), cfg.damp_alpha, cfg.damp_beta
     return c
 
 
