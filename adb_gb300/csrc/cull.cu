@@ -342,6 +342,109 @@ __device__ __forceinline__ SubLists sub_lists(const Geo& g, int sub, int I, int 
   return L;
 }
 
+// Block-wide union of float boxes (min of lo, max of hi); the result is broadcast.
+__device__ __forceinline__ void block_box_union(float* b, float* sh /* >= 6 * NT/32 + 6 */) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      float v = __shfl_xor_sync(0xffffffffu, b[c], o);
+      b[c] = c < 3 ? fminf(b[c], v) : fmaxf(b[c], v);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sh[6 * w + c] = b[c];
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) sh[c] = c < 3 ? fminf(sh[c], sh[6 * q + c]) : fmaxf(sh[c], sh[6 * q + c]);
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < 6; ++c) b[c] = sh[c];
+  __syncthreads();
+}
+
+// Keeps, in order and in place, the entries of list L[0..n) whose float box (inflated by
+// ds when `infl`) hits box `q`; returns the new length. Writes never pass reads: each
+// chunk of NT entries is read before any of it is written.
+__device__ __forceinline__ int block_compact(int* L, int n, int off, const float* boxes, bool infl, float ds,
+                                             const float* q, int* sh /* >= NT/32 + 1 */) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  int kept = 0;
+  for (int k0 = 0; k0 < n; k0 += NT) {
+    int k = k0 + threadIdx.x;
+    int id = 0;
+    bool keep = false;
+    if (k < n) {
+      id = L[k];
+      float bx[6];
+      const float* src = boxes + 6 * (off + id);
+      if (infl) finflate(src, ds, bx);
+      else
+#pragma unroll
+        for (int c = 0; c < 6; ++c) bx[c] = src[c];
+      keep = f_overlap(bx, q);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) sh[w] = __popc(m);
+    __syncthreads();
+    int pre = 0, tot = 0;
+#pragma unroll
+    for (int q2 = 0; q2 < NT / 32; ++q2) {
+      pre += q2 < w ? sh[q2] : 0;
+      tot += sh[q2];
+    }
+    if (keep) L[kept + pre + __popc(m & below)] = id;
+    kept += tot;
+    __syncthreads();
+  }
+  return kept;
+}
+
+// Shrinks the two lists of a sub-problem so that every candidate pair whose float boxes
+// hit survives: A keeps the entries hitting the union of the B boxes, then B keeps the
+// entries hitting the union of the kept A boxes (A inflated by ds when `infl`). The
+// reference's loose body boxes bin whole caps of both bodies; this leaves the part near
+// the other body.
+__device__ void refine_lists(SubLists& L, int* nA_slot, int* nB_slot, bool infl, float ds, float* shf, int* shi) {
+  float bb[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int k = threadIdx.x; k < L.nB; k += NT) {
+    const float* b = L.boxB + 6 * (L.offB + L.LB[k]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      bb[c] = fminf(bb[c], b[c]);
+      bb[c + 3] = fmaxf(bb[c + 3], b[c + 3]);
+    }
+  }
+  block_box_union(bb, shf);
+  int* LA = const_cast<int*>(L.LA);
+  int* LB = const_cast<int*>(L.LB);
+  L.nA = block_compact(LA, L.nA, L.offA, L.boxA, infl, ds, bb, shi);
+  float ba[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int k = threadIdx.x; k < L.nA; k += NT) {
+    float a[6];
+    const float* src = L.boxA + 6 * (L.offA + LA[k]);
+    if (infl) finflate(src, ds, a);
+    else
+#pragma unroll
+      for (int c = 0; c < 6; ++c) a[c] = src[c];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      ba[c] = fminf(ba[c], a[c]);
+      ba[c + 3] = fmaxf(ba[c + 3], a[c + 3]);
+    }
+  }
+  block_box_union(ba, shf);
+  L.nB = L.nA ? block_compact(LB, L.nB, L.offB, L.boxB, false, ds, ba, shi) : 0;
+  if (threadIdx.x == 0) {
+    *nA_slot = L.nA;
+    *nB_slot = L.nB;
+  }
+}
+
 // Stages one chunk of each list's float boxes in shared memory (A side inflated by
 // sqrt(dhat), rounded outward, unless `traj`).
 __device__ __forceinline__ void stage(const SubLists& L, int a0, int ca, int b0, int cb, bool inflate_a, float ds_f,
@@ -377,7 +480,7 @@ __device__ __forceinline__ bool f_hit(const float* a, const float* b) {
 //    FP64 test (MODE 0: box, lower bounds, type and distance; MODE 2: time of impact).
 template <int MODE>
 __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
-                                                    const int* cnt, const int* off, const int* lst, const float* vb,
+                                                    int* cnt, const int* off, int* lst, const float* vb,
                                                     const float* eb, const float* fb, int* sub_cnt,
                                                     unsigned long long* toi_key, unsigned long long* stage_key,
                                                     int8_t* stage_ty, int* stage_off, int* stage_total,
@@ -388,8 +491,10 @@ __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds
   __shared__ unsigned long long recK[MODE == 0 ? REC_CAP : 1];
   __shared__ int8_t recT[MODE == 0 ? REC_CAP : 1];
   __shared__ int rec_n, rec_base;
+  __shared__ float sh_box[6 * (NT / 32) + 6];
+  __shared__ int sh_cnt[NT / 32 + 1];
   const int u = blockIdx.x;
-  const int* n = cnt + 6 * u;
+  int* n = cnt + 6 * u;
   const int* o = off + 6 * u;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned below = (1u << lane) - 1u;
@@ -404,6 +509,11 @@ __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds
 #pragma unroll 1
   for (int sub = 0; sub < 3; ++sub) {
     SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, o, lst, vb, eb, fb);
+    if (L.nA == 0 || L.nB == 0) continue;
+    {
+      const int la = sub == 0 ? 0 : (sub == 1 ? 3 : 1), lb = sub == 0 ? 5 : (sub == 1 ? 2 : 4);
+      refine_lists(L, n + la, n + lb, MODE != 2, ds_f, sh_box, sh_cnt);
+    }
     if (L.nA == 0 || L.nB == 0) continue;
     int cs = 0;
 #pragma unroll 1

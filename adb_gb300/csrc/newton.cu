@@ -208,6 +208,7 @@ __global__ void __launch_bounds__(256) k_ov_reduce(int nov, const int* pt_seg, c
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int p0 = pt_seg[u], p1 = pt_seg[u + 1], e0 = ee_seg[u], e1 = ee_seg[u + 1];
   if (threadIdx.x == 0) has[u] = (p1 > p0) || (e1 > e0);
+  if (p1 == p0 && e1 == e0) return;  // no pairs: the record is never read (has[u] = 0)
   for (int c = w; c < CONTRIB; c += 8) {
     double s = 0.0;
     for (int p = p0 + lane; p < p1; p += 32) s += ptC[(size_t)c * npt + p];

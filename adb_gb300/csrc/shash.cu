@@ -192,6 +192,7 @@ __global__ void k_pt_query(Geo g, ShQuery Q, const int* off, unsigned long long*
       for (int k = l[2]; k <= u[2]; ++k) {
         unsigned b = sh_hash(i, j, k, Q.G.bits);
         for (int e = Q.bstart[b]; e < Q.bend[b]; ++e) {
+          if (e > Q.bstart[b] && Q.keys[e] == Q.keys[e - 1]) continue;  // registered twice in one bucket
           int v = (int)(Q.keys[e] & 0xffffffffull);
           int I = g.vbody[v];
           if (I == J || g.bscene[I] != g.bscene[J]) continue;
@@ -255,6 +256,7 @@ __global__ void k_ee_query(Geo g, ShQuery Q, const int* off, unsigned long long*
       for (int k = l[2]; k <= u[2]; ++k) {
         unsigned b = sh_hash(i, j, k, Q.G.bits);
         for (int e = Q.bstart[b]; e < Q.bend[b]; ++e) {
+          if (e > Q.bstart[b] && Q.keys[e] == Q.keys[e - 1]) continue;  // registered twice in one bucket
           int ei = (int)(Q.keys[e] & 0xffffffffull);
           int ia0 = g.ev[2 * ei], ia1 = g.ev[2 * ei + 1];
           int I = g.vbody[ia0];
