@@ -115,6 +115,19 @@ class ABD:
     def iter(self, v: int):
         L.lib().abd_set_iter(self._h, int(v))
 
+    def set_friction(self, mu: float):
+        L.check(L.lib().abd_set_friction(self._h, float(mu)), self._h, "abd_set_friction")
+
+    def adjoint_frame(self, q_t: np.ndarray, v_t: np.ndarray, q_next: np.ndarray, gq_next: np.ndarray):
+        """(dL/dq_t, dL/dv_t, dL/dmu) of one converged frame from dL/dq_{t+1}."""
+        a = [np.ascontiguousarray(x, np.float64) for x in (q_t, v_t, q_next, gq_next)]
+        gq, gv = np.zeros((self.nb, 12)), np.zeros((self.nb, 12))
+        gm = C.c_double(0.0)
+        rc = L.lib().abd_adjoint_frame(self._h, *[L.dptr(x) for x in a], L.dptr(gq), L.dptr(gv), C.byref(gm))
+        if rc not in (0, 6):
+            L.check(rc, self._h, "abd_adjoint_frame")
+        return gq, gv, gm.value
+
     # --- per-kernel device timing -----------------------------------------------------
     @property
     def n_scenes(self) -> int:

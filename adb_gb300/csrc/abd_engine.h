@@ -85,12 +85,15 @@ struct PairSet {
   DBuf<double> vg_lam;
 };
 
+enum { TERM_INERTIA = 1, TERM_BARRIER = 2, TERM_FRICTION = 4, TERM_ALL = 7 };
 struct Params {
   double dhat, kappa, d_sqrt, eps_x, ortho_kappa, ground_offset, dt, gravity_y;
   double mu, epsv, max_uk;
   double damp_alpha, damp_beta;  // "damping": {alpha, beta}
   int psd, pt_fric, ee_fric, vg_fric, ground, pt, ee;
   int damp;                      // "damping": {enable}
+  int terms;                     // TERM_* mask of the energy terms assembled (all by default)
+  int exact;                     // 1: exact ground Hessian (adjoint systems)
 };
 
 // Culling scratch shared by all culls of a handle.
@@ -245,6 +248,10 @@ void dots(const Geo& g, const double* dq, const double* grad, NewtonBufs& nb, do
 void scene_diff(const Geo& g, const double* a, const double* b, NewtonBufs& nb, double* out, cudaStream_t s);
 void launch_copy_scene(const Geo& g, double* dst, const double* src, const int* on, cudaStream_t st);
 void launch_scale_scene(const Geo& g, double* v, const double* f, cudaStream_t st);
+// y = H x with the system assembled last on S (no synchronisation)
+void spmv(const Geo& g, const PairSet& S, NewtonBufs& nb, const double* x, double* y, cudaStream_t st);
+// out = C^T w for the ground-friction multiplier coupling of an adjoint system
+void vg_lag_adjoint(const Geo& g, const Params& P, const PairSet& S, const double* w, double* out, cudaStream_t st);
 void launch_q_update_scene(const Geo& g, double* q, const double* dq, const double* alpha, cudaStream_t st);
 void launch_frame_end(double* q, double* q0, double* dqdt, int n, double dt, cudaStream_t st);
 void launch_copy(double* dst, const double* src, int n, cudaStream_t st);

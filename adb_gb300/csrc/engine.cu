@@ -183,6 +183,8 @@ struct Engine {
     P.ground = c->ground;
     P.pt = c->pt;
     P.ee = c->ee;
+    P.terms = TERM_ALL;
+    P.exact = 0;
     P.damp = c->damping;
     P.damp_alpha = c->damp_alpha;
     P.damp_beta = c->damp_beta;
@@ -827,6 +829,97 @@ int abd_newton_system(abd_handle* h, const double* q, double* grad, double* diag
     }
     if (n_off) *n_off = k;
     return (int)ABD_OK;
+  });
+}
+
+int abd_set_friction(abd_handle* h, double mu) {
+  if (!h || !(mu >= 0.0)) return ABD_ERR_INVALID;
+  h->e.P.mu = mu;
+  h->e.cfg.mu = mu;
+  return ABD_OK;
+}
+
+// Adjoint of one converged frame by implicit differentiation. At the frame's solution
+// q_{t+1} the gradient r(q; q_t, v_t, mu) of the incremental potential vanishes, so
+// dL/dtheta = -w^T dr/dtheta with J^T w = dL/dq_{t+1}, J the Jacobian of r at q_{t+1}:
+// the exact Hessian (no PSD projection, no damping, the ground barrier's full second
+// derivative) plus the coupling through the ground-friction multipliers, which follow the
+// vertex heights at the solution (folded in by a fixed-point iteration around the PCG).
+// dr/dq_t = -M - mu K (inertia through q_tilde, friction through the reference positions
+// x(q_t)), dr/dv_t = -dt M, dr/dmu = r_friction / mu, with K and r_friction assembled at
+// mu = 1. Point-triangle and edge-edge friction multipliers and tangent bases are held
+// fixed, as the forward Newton iteration holds them.
+int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const double* q_next,
+                      const double* gq_next, double* gq_t, double* gv_t, double* gmu) {
+  if (!h || !q_t || !v_t || !q_next || !gq_next || !gq_t || !gv_t) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    Engine& e = h->e;
+    const int nb = e.nb;
+    size_t n = 12 * (size_t)nb;
+    CK(cudaMemcpyAsync(e.q0.p, q_t, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
+    CK(cudaMemcpyAsync(e.dqdt.p, v_t, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
+    CK(cudaMemcpyAsync(e.q.p, q_next, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
+    CK(cudaMemsetAsync(e.dq.p, 0, n * sizeof(double), e.s));
+    abd::Geo g = e.geo();
+    abd::PairSet& S = e.sets[e.cur];
+    abd::launch_project(g, 0, 0.0, e.s);
+    e.cull_set(g, 1, S);
+    abd::Params Pe = e.P;
+    Pe.psd = 0;
+    Pe.damp = 0;
+    Pe.exact = 1;
+    Pe.terms = abd::TERM_ALL;
+    abd::assemble(g, Pe, S, e.nbufs, e.s);
+    e.put_on(std::vector<char>(e.ns, 1));
+    // J^T w = gq_next with J = H + C by the fixed point H w_{k+1} = gq_next - C^T w_k
+    std::vector<double> w(n, 0.0), y(n), gf(n), mass(nb), Ic(nb), ctw(n, 0.0), rhs(n), wprev(n);
+    int st = 0;
+    for (int it = 0; it < 50; ++it) {
+      for (size_t k = 0; k < n; ++k) rhs[k] = gq_next[k] - ctw[k];
+      CK(cudaMemcpyAsync(e.nbufs.grad.p, rhs.data(), n * sizeof(double), cudaMemcpyHostToDevice, e.s));
+      abd::pcg_solve(g, S, e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.sc_on.p, e.dq.p, e.s, &st, nullptr);
+      if (st == ABD_ERR_NOT_SPD) return st;
+      wprev = w;
+      CK(cudaMemcpyAsync(w.data(), e.nbufs.x.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
+      CK(cudaStreamSynchronize(e.s));
+      if (!(e.P.mu > 0.0 && e.cfg.ground && e.cfg.vg_fric && S.nvg > 0)) break;
+      double dn = 0.0, wn = 0.0;
+      for (size_t k = 0; k < n; ++k) {
+        dn += (w[k] - wprev[k]) * (w[k] - wprev[k]);
+        wn += w[k] * w[k];
+      }
+      if (it > 0 && dn <= 1e-28 * wn) break;
+      abd::vg_lag_adjoint(g, Pe, S, e.nbufs.x.p, e.nbufs.qv.p, e.s);  // PCG scratch between solves
+      CK(cudaMemcpyAsync(ctw.data(), e.nbufs.qv.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
+      CK(cudaStreamSynchronize(e.s));
+    }
+    // friction terms alone at mu = 1: K w and r_friction / mu
+    abd::Params Pf = Pe;
+    Pf.terms = abd::TERM_FRICTION;
+    Pf.mu = 1.0;
+    abd::assemble(g, Pf, S, e.nbufs, e.s);
+    abd::spmv(g, S, e.nbufs, e.nbufs.x.p, e.nbufs.r.p, e.s);
+    CK(cudaMemcpyAsync(y.data(), e.nbufs.r.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
+    CK(cudaMemcpyAsync(gf.data(), e.nbufs.grad.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
+    CK(cudaMemcpyAsync(mass.data(), e.mass.p, nb * sizeof(double), cudaMemcpyDeviceToHost, e.s));
+    CK(cudaMemcpyAsync(Ic.data(), e.Ic.p, nb * sizeof(double), cudaMemcpyDeviceToHost, e.s));
+    CK(cudaStreamSynchronize(e.s));
+    double gm = 0.0, mu = e.P.mu, dt = e.P.dt;
+    for (int b = 0; b < nb; ++b)
+      for (int i = 0; i < 12; ++i) {
+        size_t k = 12 * (size_t)b + i;
+        if (mass[b] < 0.0) {  // static: q_{t+1} = q_t
+          gq_t[k] = gq_next[k];
+          gv_t[k] = 0.0;
+          continue;
+        }
+        double m = i < 3 ? mass[b] : Ic[b];
+        gq_t[k] = m * w[k] + mu * y[k];
+        gv_t[k] = dt * m * w[k];
+        gm -= gf[k] * w[k];
+      }
+    if (gmu) *gmu = gm;
+    return st;
   });
 }
 

@@ -85,7 +85,12 @@ __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, i
     }
     lam = -barrier_b1(d, bp) * 2 * sqrt(d);
     pair_reduced(kind, ty, X, d, bp, P.eps_x, P.psd != 0, S, gv);
-    bool fric = (kind == 0) ? P.pt_fric : P.ee_fric;
+    if (!(P.terms & TERM_BARRIER)) {
+      for (int i = 0; i < 9; ++i)
+        for (int j = 0; j < 9; ++j) S[i][j] = 0.0;
+      for (int i = 0; i < 4; ++i) gv[i] = fd3(0, 0, 0);
+    }
+    bool fric = ((kind == 0) ? P.pt_fric : P.ee_fric) && (P.terms & TERM_FRICTION);
     if (fric) pair_friction(fr, uk, lam, FrictionP{P.mu, P.epsv, P.max_uk}, S, gv);
   } else {
     fr.c0 = fd3(0, 0, 0);
@@ -259,7 +264,9 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
   }
   double mi = (i < 3) ? m : g.Ic[b];
   double kap = 4.0 * P.ortho_kappa;
-  if (is_h) {
+  if (!(P.terms & TERM_INERTIA)) {
+    // no inertia / orthogonality terms (adjoint of the friction terms alone)
+  } else if (is_h) {
     val = (i == j) ? mi : 0.0;
     if (k >= 1 && l >= 1) {
       d3 ak = mk(q[3 * k], q[3 * k + 1], q[3 * k + 2]);
@@ -288,6 +295,7 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
     if (i == 1) qt += dt * dt * P.gravity_y;
     val = dt * dt * og + mi * (q[i] - qt);
   }
+  const bool vg_bar = (P.terms & TERM_BARRIER) != 0, vg_fr = (P.terms & TERM_FRICTION) && P.vg_fric;
   // vertex-ground terms (barrier.cpp:31-69, friction with basis (e_x, e_z))
   BarrierP bp{P.dhat, P.kappa};
   for (int kk = vg_seg[b]; kk < vg_seg[b + 1]; ++kk) {
@@ -305,16 +313,18 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
     double xt[4] = {1.0, g.rest[3 * v], g.rest[3 * v + 1], g.rest[3 * v + 2]};
     double uk[2] = {g.X[v] - g.X0[v], g.X[2 * g.nv + v] - g.X0[2 * g.nv + v]};
     double gs = 0.0, M[2][2] = {{0, 0}, {0, 0}};
-    if (P.vg_fric) friction_2x2(uk, lamv, FrictionP{P.mu, P.epsv, P.max_uk}, gs, M);
+    if (vg_fr) friction_2x2(uk, lamv, FrictionP{P.mu, P.epsv, P.max_uk}, gs, M);
     if (is_h) {
       double N = 0.0;
-      if (r == 1 && s == 1) N = b2 * (2 * _d) * (2 * _d);
+      // the reference drops b' d'' = 2 b' from the ground Hessian (barrier.cpp:62-69); the
+      // exact Hessian (adjoint systems) keeps it
+      if (r == 1 && s == 1 && vg_bar) N = b2 * (2 * _d) * (2 * _d) + (P.exact ? 2 * b1 : 0.0);
       int rr = (r == 0) ? 0 : (r == 2 ? 1 : -1), ss = (s == 0) ? 0 : (s == 2 ? 1 : -1);
       if (rr >= 0 && ss >= 0) N += M[rr][ss];
       val += xt[k] * xt[l] * N;
     } else {
       double F = 0.0;
-      if (r == 1) F = b1 * 2 * _d;
+      if (r == 1 && vg_bar) F = b1 * 2 * _d;
       if (r == 0) F += gs * uk[0];
       if (r == 2) F += gs * uk[1];
       val += xt[k] * F;
@@ -952,6 +962,63 @@ __global__ void k_copy_scene(double* dst, const double* src, int n, const int* b
   if (i < n && on[bscene[i / 12]]) dst[i] = src[i];
 }
 
+// Transpose of the ground-friction multiplier coupling (adjoint systems): the lagged
+// multiplier lam(y) = -2 b'(d) (y + off) of each vertex-ground pair moves with the
+// vertex height at the solution, which adds C = (r_f / lam) (dlam/dy J_y)^T to the
+// Jacobian of the gradient. out = C^T w, one thread per body.
+__global__ void k_vg_lag_adj(Geo g, Params P, const int* vg, const int* vg_seg, const double* w, double* out) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.nb) return;
+  double acc[4] = {0, 0, 0, 0};
+  const double* wb = w + 12 * b;
+  if (g.mass[b] > 0.0 && P.ground && P.vg_fric) {
+    BarrierP bp{P.dhat, P.kappa};
+    for (int kk = vg_seg[b]; kk < vg_seg[b + 1]; ++kk) {
+      int v = g.v_off[b] + vg[2 * kk + 1];
+      double _d = g.X[g.nv + v] + P.ground_offset;
+      double dd = _d * _d;
+      if (!(dd < P.dhat)) continue;
+      double b1 = barrier_b1(dd, bp), b2 = barrier_b2(dd, bp);
+      double lam = -b1 * 2 * _d;
+      if (lam == 0.0) continue;
+      double dlam = -2.0 * (2.0 * b2 * dd + b1);
+      double uk[2] = {g.X[v] - g.X0[v], g.X[2 * g.nv + v] - g.X0[2 * g.nv + v]};
+      double gs = 0.0, M[2][2];
+      friction_2x2(uk, lam, FrictionP{P.mu, P.epsv, P.max_uk}, gs, M);
+      double xt[4] = {1.0, g.rest[3 * v], g.rest[3 * v + 1], g.rest[3 * v + 2]};
+      double wx = 0.0, wz = 0.0;
+      for (int k = 0; k < 4; ++k) {
+        wx += xt[k] * wb[3 * k];
+        wz += xt[k] * wb[3 * k + 2];
+      }
+      double c = dlam * (gs / lam) * (uk[0] * wx + uk[1] * wz);
+      for (int k = 0; k < 4; ++k) acc[k] += xt[k] * c;
+    }
+  }
+  for (int k = 0; k < 4; ++k) {
+    out[12 * b + 3 * k] = 0.0;
+    out[12 * b + 3 * k + 1] = acc[k];
+    out[12 * b + 3 * k + 2] = 0.0;
+  }
+}
+
+// y = H x over the assembled block-sparse matrix (diagonal blocks D, off-diagonal blocks
+// in the per-overlap records), one thread per (body, row) slot.
+__global__ void k_spmv(int nb, const int* row_ptr, const int* col, const int* upidx, const int* has,
+                       const double* ovr, const double* D, const double* x, double* y) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int body = s >> 4, row = s & 15;
+  if (body >= nb || row >= 12) return;
+  PcgArgs a;
+  a.row_ptr = row_ptr;
+  a.col = col;
+  a.upidx = upidx;
+  a.has = has;
+  a.ovr = ovr;
+  a.D = D;
+  y[12 * body + row] = row_spmv(a, body, row, x);
+}
+
 // v *= f[scene of body]
 __global__ void k_scale_scene(double* v, int n, const int* bscene, const double* f) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1146,6 +1213,15 @@ void launch_copy_scene(const Geo& g, double* dst, const double* src, const int* 
   int n = 12 * g.nb;
   if (n <= 0) return;
   KLAUNCH(K_VEC, st, k_copy_scene<<<nblk(n, 256), 256, 0, st>>>(dst, src, n, g.bscene, on));
+}
+
+void spmv(const Geo& g, const PairSet& S, NewtonBufs& B, const double* x, double* y, cudaStream_t st) {
+  KLAUNCH(K_PCG, st, k_spmv<<<nblk((long long)g.nb * 16, 256), 256, 0, st>>>(g.nb, S.row_ptr.p, S.col.p, S.upidx.p,
+                                                                            B.has.p, B.ovr.p, B.D.p, x, y));
+}
+
+void vg_lag_adjoint(const Geo& g, const Params& P, const PairSet& S, const double* w, double* out, cudaStream_t st) {
+  KLAUNCH(K_BODY_SYSTEM, st, k_vg_lag_adj<<<nblk(g.nb, 128), 128, 0, st>>>(g, P, S.vg.p, S.vg_seg.p, w, out));
 }
 
 void launch_scale_scene(const Geo& g, double* v, const double* f, cudaStream_t st) {

@@ -517,16 +517,18 @@ def batched_scenes(n_scenes: int = 256, seed: int = 0, lo: int = 4, hi: int = 12
     return sb.build()
 
 
-def diff_grid(seed: int = 0) -> Scene:
-    """64 subdivision-2 icospheres on a 4x4x4 grid with spacing 1.2."""
+def diff_grid(seed: int = 0, n: int = 4, spacing: float = 1.2, lift: float = 0.6) -> Scene:
+    """n^3 subdivision-2 icospheres on an n x n x n grid (64 with spacing 1.2 by default),
+    the lowest layer `lift` above the ground."""
     rng = np.random.default_rng(seed)
     ico = icosphere_mesh(2, 0.5)
     m = 1000.0 * ico.volume
     sb = SceneBuilder()
-    for iy in range(4):
-        for ix in range(4):
-            for iz in range(4):
-                p = ((ix - 1.5) * 1.2, 0.6 + iy * 1.2 + GROUND_SHIFT, (iz - 1.5) * 1.2)
+    c = (n - 1) / 2
+    for iy in range(n):
+        for ix in range(n):
+            for iz in range(n):
+                p = ((ix - c) * spacing, lift + iy * spacing + GROUND_SHIFT, (iz - c) * spacing)
                 sb.add(ico, p, random_rotation(rng), mass=m)
     return sb.build()
 

@@ -169,13 +169,40 @@ def batched_vs_looped(frames=5, warm_frames=30, n_scenes=256, loop_budget_s=30.0
             "newton_iters": bst.newton_iters, "max_pt": bst.n_pt, "max_ee": bst.n_ee}
 
 
-def cpu_baseline_sample(sc, cfg, q0, qd, newton_per_frame, sample_iters=6):
+def adjoint_cost(n_steps=20, every=5):
+    """Forward and backward time of a differentiable rollout of the 64-icosphere grid
+    (mu 0.3): n_steps frames forward, then the adjoint (recomputing each checkpointed
+    segment), timed on the wall clock."""
+    import torch
+    from adb_gb300 import scene as S
+    from adb_gb300.abd import ABD
+    from adb_gb300.adjoint import rollout
+    sc = S.diff_grid(seed=0)
+    cfg = S.workload_config("diff")
+    sim = ABD(sc, cfg)
+    q0 = torch.tensor(sc.q0, dtype=torch.float64, requires_grad=True)
+    v0 = torch.zeros_like(q0, requires_grad=True)
+    mu = torch.tensor(cfg.mu, dtype=torch.float64, requires_grad=True)
+    t0 = time.perf_counter()
+    qT, _ = rollout(sim, q0, v0, mu, n_steps, every)
+    t_fwd = time.perf_counter() - t0
+    loss = (qT[:, :3] ** 2).sum()
+    t0 = time.perf_counter()
+    loss.backward()
+    t_bwd = time.perf_counter() - t0
+    sim.close()
+    return {"scene": "64 icosphere-s2 grid, mu %.1f" % cfg.mu, "frames": n_steps, "checkpoint_every": every,
+            "forward_s": t_fwd, "backward_s": t_bwd, "backward_over_forward": t_bwd / t_fwd}
+
+
+def cpu_baseline_sample(sc, cfg, q0, qd, newton_per_frame, ls_per_frame, sample_iters=6):
     """The CPU restatement on all host cores, timed on a bounded sample of one frame.
 
-    The sample is the first `sample_iters` Newton iterations (each with its line search and
-    re-culls) of the frame that starts from (q0, qd); frames/s is scaled from the time per
-    Newton iteration by the Newton iterations per frame the GPU run took on the same frames
-    (the two paths take identical iteration counts, which the parity tests check)."""
+    The sample is the first `sample_iters` Newton iterations of the frame that starts from
+    (q0, qd). Its time splits into the Newton part (assembly, solve, step bound) per
+    iteration and the line search per trial; frames/s is scaled from those by the Newton
+    iterations and line-search trials per frame the GPU run took on the same frames (the
+    two paths take identical counts, which the parity tests check)."""
     import dataclasses
     from oracle import oracle as O
     cores = os.cpu_count() or 1
@@ -186,9 +213,11 @@ def cpu_baseline_sample(sc, cfg, q0, qd, newton_per_frame, sample_iters=6):
     t0 = time.perf_counter()
     st = sim.step(1)
     secs = time.perf_counter() - t0
-    its = st.newton_iters
-    per_it = secs / max(its, 1)
-    return 1.0 / (per_it * newton_per_frame), cores, its, secs
+    its, trials = max(st.newton_iters, 1), max(st.ls_trials, 1)
+    t_newton = (st.t_ipc + st.t_solver + st.t_ccd) / its
+    t_trial = st.t_ls / trials
+    frame_s = newton_per_frame * t_newton + ls_per_frame * t_trial
+    return 1.0 / frame_s, cores, its, trials, secs
 
 
 def run_reference(args):
@@ -331,12 +360,18 @@ def run_gb300(args):
         }
         if not args.no_batched:
             line["batched"] = batched_vs_looped()
+            try:
+                line["adjoint"] = adjoint_cost()
+            except ImportError as ex:  # torch missing on this host
+                line["adjoint"] = {"unavailable": str(ex)}
         if world == 1 and not args.no_cpu_baseline:
             npf = st.newton_iters / max(args.steps, 1)
-            v, cores, its, secs = cpu_baseline_sample(sc, cfg, start_q, start_qd, npf)
+            lpf = st.ls_trials / max(args.steps, 1)
+            v, cores, its, trials, secs = cpu_baseline_sample(sc, cfg, start_q, start_qd, npf, lpf)
             line["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": cores, "kind": "port",
-                                    "sample": ("first %d Newton iterations of the first timed frame (%.1f s), "
-                                               "scaled by %.2f Newton iterations per frame" % (its, secs, npf))}
+                                    "sample": ("first %d Newton iterations (%d line-search trials) of the first "
+                                               "timed frame (%.1f s), scaled per phase to %.2f iterations and %.2f "
+                                               "trials per frame" % (its, trials, secs, npf, lpf))}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -121,6 +121,17 @@ int abd_get_counts(abd_handle* h, int* n_bodies, int* n_vertices, int* n_edges, 
  * abd_get_iter, of every scene for abd_set_iter. */
 int abd_get_iter(abd_handle* h);
 int abd_set_iter(abd_handle* h, int iter);
+/* Friction coefficient of the handle (config "mu"), e.g. between differentiated rollouts. */
+int abd_set_friction(abd_handle* h, double mu);
+/* Adjoint of one converged frame (no reference counterpart: the reference has no
+ * derivatives). The frame maps the frame-start state (q_t, v_t) and mu to q_{t+1}; given
+ * gq_next = dL/dq_{t+1} it assembles the exact Jacobian of the frame's optimality condition
+ * at q_{t+1} (no PSD projection, no damping, ground-friction multipliers following the
+ * vertex heights; point-triangle and edge-edge friction multipliers and tangent bases held
+ * fixed), solves it with the block-sparse PCG and returns gq_t = dL/dq_t, gv_t = dL/dv_t
+ * and *gmu = dL/dmu (gmu may be NULL). All arrays are n_bodies * 12 host doubles. */
+int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const double* q_next,
+                      const double* gq_next, double* gq_t, double* gv_t, double* gmu);
 /* Batched mode (no reference counterpart: the reference steps one scene per ABD object).
  * Number of scenes of the handle, and per-scene counts (arrays of that length, any may be
  * NULL) accumulated over the frames of the last abd_step call, plus each scene's

@@ -1,0 +1,82 @@
+"""Adjoint rollouts (torch.autograd.Function over the GPU step) against central finite
+differences of the oracle's rollout (the CPU restatement of the reference step).
+
+Loss: sum of squared distances of the bodies' translations after the rollout to seeded
+targets. Newton runs to a tight tolerance so that the finite differences resolve the
+converged map. The adjoint is exact without friction and with ground friction (its
+multiplier's dependence on the vertex height is included); the multipliers and tangent
+bases of point-triangle and edge-edge friction are held fixed, so contact friction between
+bodies is not covered by this check."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from adb_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def O(gpu_lib, oracle_lib):
+    return oracle_lib
+
+
+def setup(mu, contact_friction=True):
+    sc = S.diff_grid(seed=1, n=2, spacing=1.05, lift=0.56)
+    cfg = dataclasses.replace(S.workload_config("diff"), mu=mu, tol=1e-12, pt_friction=contact_friction,
+                              ee_friction=contact_friction)
+    rng = np.random.default_rng(7)
+    target = sc.q0[:, :3] + rng.uniform(-0.3, 0.3, (sc.n_bodies, 3))
+    v0 = np.zeros_like(sc.q0)
+    v0[:, :3] = rng.normal(0.0, 0.5, (sc.n_bodies, 3))
+    v0[:, 1] -= 1.0
+    return sc, cfg, target, v0
+
+
+def oracle_loss(O, sc, cfg, q0, v0, mu, target, n):
+    o = O.OracleSim(sc, dataclasses.replace(cfg, mu=mu))
+    o.set_state(q0, v0)
+    o.step(n)
+    q, _ = o.state()
+    return float(((q[:, :3] - target) ** 2).sum())
+
+
+@pytest.mark.parametrize("mu,contact_friction,bound", [(0.0, True, 1e-5), (0.3, False, 1e-5)])
+def test_adjoint_matches_oracle_finite_differences(O, mu, contact_friction, bound):
+    from adb_gb300.abd import ABD
+    from adb_gb300.adjoint import rollout
+    sc, cfg, target, v0 = setup(mu, contact_friction)
+    n = 12
+    sim = ABD(sc, cfg)
+    q0t = torch.tensor(sc.q0, dtype=torch.float64, requires_grad=True)
+    v0t = torch.tensor(v0, dtype=torch.float64, requires_grad=True)
+    mut = torch.tensor(mu, dtype=torch.float64, requires_grad=True)
+    qT, _ = rollout(sim, q0t, v0t, mut, n, every=4)
+    loss = ((qT[:, :3] - torch.tensor(target)) ** 2).sum()
+    loss.backward()
+    L0 = oracle_loss(O, sc, cfg, sc.q0, v0, mu, target, n)
+    assert abs(float(loss.detach()) - L0) <= 1e-8 * abs(L0)
+    rng = np.random.default_rng(3)
+    h = 1e-5
+    pairs = []
+    for k in range(3):
+        d = rng.normal(size=v0.shape)
+        d[:, 3:] = 0.0
+        d /= np.linalg.norm(d)
+        fd = (oracle_loss(O, sc, cfg, sc.q0, v0 + h * d, mu, target, n) -
+              oracle_loss(O, sc, cfg, sc.q0, v0 - h * d, mu, target, n)) / (2 * h)
+        ad = float((v0t.grad.numpy() * d).sum())
+        print("adjoint v0 direction %d: %.10g fd %.10g" % (k, ad, fd))
+        pairs.append((ad, fd))
+    # errors relative to the largest directional derivative (the finite differences of a
+    # converged Newton solve resolve derivatives to a fraction of the gradient's size)
+    scale = max(abs(fd) for _, fd in pairs)
+    for k, (ad, fd) in enumerate(pairs):
+        assert abs(ad - fd) <= bound * scale, (k, ad, fd, scale)
+    if mu > 0:
+        fd = (oracle_loss(O, sc, cfg, sc.q0, v0, mu + h, target, n) -
+              oracle_loss(O, sc, cfg, sc.q0, v0, mu - h, target, n)) / (2 * h)
+        print("adjoint mu: %.10g fd %.10g" % (float(mut.grad), fd))
+        assert abs(float(mut.grad) - fd) <= bound * abs(fd), (float(mut.grad), fd)
