@@ -46,6 +46,7 @@ struct Geo;
 __host__ __device__ inline bool scene_on(const Geo& g, int body);
 struct Geo {
   int nb, nv, ne, nf;
+  int max_prims;                        // most vertices + edges + faces of one body
   const int *v_off, *e_off, *f_off;     // nb + 1
   const double* rest;                   // nv * 3 (x, y, z per vertex)
   const int* vbody;                     // nv
@@ -222,8 +223,12 @@ struct NewtonBufs {
   DBuf<double> ovr;          // nov * CONTRIB
   DBuf<int> has;             // nov
   DBuf<double> D, Dinv, grad;
-  DBuf<double> x, r, z, p, qv;
-  DBuf<double> bpA, bpB;     // per-body partial sums of the PCG
+  DBuf<double> x, r, z, p, qv;   // p: two buffers (iteration parity)
+  DBuf<double> Hrow;         // row-block copy of the system for the PCG
+  DBuf<int> rcol, rn;
+  DBuf<double> gpA, gpB;     // per-group partial sums of the PCG
+  DBuf<int> grp_body, grp_n, grp_scene, sc_gbeg, sc_gend;  // PCG body groups (pcg_groups)
+  int ngrp = 0;
   DBuf<double> sc_rz, sc_bb; // per-scene CG scalars
   DBuf<int> sc_conv, sc_iters, n_active;
   DBuf<double> red;          // chunk partial sums of the energies
@@ -236,6 +241,9 @@ struct NewtonBufs {
 void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& nb, cudaStream_t s);
 // Solves H x = grad per scene (scenes with sc_on[s] == 0 get x = 0); dq = -x. Returns the
 // iterations of the longest scene; scene_iters (host, ns) receives each scene's count.
+// Body groups of the PCG (consecutive bodies of one scene, cut from the scene's first
+// body); called once per handle with the scenes' body ranges.
+void pcg_groups(const std::vector<int>& sc_beg, const std::vector<int>& sc_end, NewtonBufs& nb, cudaStream_t s);
 int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& nb, double rel_tol, int max_iter, const int* sc_on, double* dq,
               cudaStream_t s, int* status, int* scene_iters);
 // Line-search energy of every scene at the trial configuration (X must hold q + alpha dq):

@@ -219,6 +219,21 @@ __device__ __forceinline__ box fbox_exact(const Geo& g, int f, int traj) {
 
 // 4. binning: one warp per (overlap, side); kinds per side: vertices, edges, faces.
 // list slot k of overlap u: 0 vi, 1 ei, 2 fi, 3 vj, 4 ej, 5 fj.
+// Binning passes: BIN_COUNT counts each list, BIN_WRITE writes it at offsets from a scan
+// of those counts, BIN_ONCE writes it at offsets sized by the body's primitive counts and
+// stores the count (one pass instead of two when that capacity fits).
+enum { BIN_COUNT = 0, BIN_WRITE = 1, BIN_ONCE = 2 };
+
+// Capacity of list slot (overlap u, side, kind): the primitive count of that body.
+__global__ void k_bin_caps(Geo g, int nov, const int* ovI, const int* ovJ, int* cap) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 6 * nov) return;
+  int u = t / 6, side = (t / 3) & 1, kind = t % 3;
+  int body = side ? ovJ[u] : ovI[u];
+  const int* o = kind == 0 ? g.v_off : (kind == 1 ? g.e_off : g.f_off);
+  cap[t] = o[body + 1] - o[body];
+}
+
 __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const int* ovJ, const double* ovcull,
                       const float* ovcull_f, const float* vb, const float* eb, const float* fb, int* cnt,
                       const int* off, int* lst) {
@@ -226,9 +241,18 @@ __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const 
   if (warp >= 2 * nov) return;
   int u = warp >> 1, side = warp & 1;
   int body = side ? ovJ[u] : ovI[u];
-  float cf[6];
+  float cf[6], ci[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) cf[k] = ovcull_f[6 * u + k];
+  // Float bounds inside the FP64 cull box: cull.lo <= ci[0..2], cull.hi >= ci[3..5]. The
+  // float box of a primitive is (rd(lo), ru(hi)) of its FP64 box, so rd(lo) < ci_hi gives
+  // lo <= nextup(rd(lo)) <= ci_hi <= cull.hi; a primitive passing that on all six sides
+  // overlaps the cull box exactly and needs no FP64 test.
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    ci[k] = nextafterf(cf[k], INFINITY);
+    ci[k + 3] = nextafterf(cf[k + 3], -INFINITY);
+  }
   box cull{mk(ovcull[6 * u], ovcull[6 * u + 1], ovcull[6 * u + 2]),
            mk(ovcull[6 * u + 3], ovcull[6 * u + 4], ovcull[6 * u + 5])};
   unsigned below = (1u << lane) - 1u;
@@ -240,19 +264,25 @@ __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const 
     else if (kind == 1) { beg = g.e_off[body]; end = g.e_off[body + 1]; fbx = eb; }
     else { beg = g.f_off[body]; end = g.f_off[body + 1]; fbx = fb; }
     int slot = u * 6 + side * 3 + kind;
-    int c = 0, base = pass ? off[slot] : 0;
+    int c = 0, base = pass != BIN_COUNT ? off[slot] : 0;
     for (int k0 = beg; k0 < end; k0 += 32) {
       int k = k0 + lane;
       bool hit = false;
-      if (k < end && f_overlap(cf, fbx + 6 * k)) {
-        box b = (kind == 0) ? vbox_exact(g, k, traj) : (kind == 1 ? ebox_exact(g, k, traj) : fbox_exact(g, k, traj));
-        hit = overlaps(cull, b);
+      if (k < end) {
+        const float* q = fbx + 6 * k;
+        if (f_overlap(cf, q)) {
+          hit = q[0] < ci[3] && q[1] < ci[4] && q[2] < ci[5] && q[3] > ci[0] && q[4] > ci[1] && q[5] > ci[2];
+          if (!hit) {
+            box b = (kind == 0) ? vbox_exact(g, k, traj) : (kind == 1 ? ebox_exact(g, k, traj) : fbox_exact(g, k, traj));
+            hit = overlaps(cull, b);
+          }
+        }
       }
       unsigned m = __ballot_sync(0xffffffffu, hit);
-      if (pass && hit) lst[base + c + __popc(m & below)] = k - beg;
+      if (pass != BIN_COUNT && hit) lst[base + c + __popc(m & below)] = k - beg;
       c += __popc(m);
     }
-    if (!pass && lane == 0) cnt[slot] = c;
+    if (pass != BIN_WRITE && lane == 0) cnt[slot] = c;
   }
 }
 
@@ -915,17 +945,24 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
     cs.bin_cnt.ensure(6 * (size_t)nov + 6);
     cs.bin_off.ensure(6 * (size_t)nov + 6);
     int nw = 2 * nov;
-    KLAUNCH(K_BIN, s, k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, 0, traj, S.ovI.p, S.ovJ.p, cs.ovcull.p,
-                                                        cs.ovcull_f.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.bin_cnt.p,
-                                                        nullptr, nullptr));
+    // list capacity = the primitive counts of both bodies of every overlap; when it fits
+    // (at most 2^28 entries) one binning pass writes the lists in place
+    bool once = 2ll * nov * g.max_prims < (1ll << 28);
+    if (once) {
+      KLAUNCH(K_BIN, s, k_bin_caps<<<nblk(6ll * nov, 256), 256, 0, s>>>(g, nov, S.ovI.p, S.ovJ.p, cs.bin_cnt.p));
+    } else {
+      KLAUNCH(K_BIN, s, k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, BIN_COUNT, traj, S.ovI.p, S.ovJ.p,
+                                                          cs.ovcull.p, cs.ovcull_f.p, cs.vbox.p, cs.ebox.p,
+                                                          cs.fbox.p, cs.bin_cnt.p, nullptr, nullptr));
+    }
     scan_exclusive_int(cs.bin_cnt.p, cs.bin_off.p, 6 * nov, d_tot + 2, s, cs.vflag_cnt);
     CK(cudaMemcpyAsync(cs.h_small + 2, d_tot + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     nlst = cs.h_small[2];
     cs.lst.ensure((size_t)nlst + 1);
-    KLAUNCH(K_BIN, s, k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, 1, traj, S.ovI.p, S.ovJ.p, cs.ovcull.p,
-                                                        cs.ovcull_f.p, cs.vbox.p, cs.ebox.p, cs.fbox.p, cs.bin_cnt.p,
-                                                        cs.bin_off.p, cs.lst.p));
+    KLAUNCH(K_BIN, s, k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, once ? BIN_ONCE : BIN_WRITE, traj,
+                                                        S.ovI.p, S.ovJ.p, cs.ovcull.p, cs.ovcull_f.p, cs.vbox.p,
+                                                        cs.ebox.p, cs.fbox.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p));
   }
   float ds_f = float_round_up(P.d_sqrt);
   NarrowOut no{};

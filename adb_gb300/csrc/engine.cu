@@ -80,6 +80,7 @@ struct Engine {
   abd_config cfg;
   Params P;
   int nb = 0, nv = 0, ne = 0, nf = 0;
+  int max_prims = 0;                             // most vertices + edges + faces of one body
   cudaStream_t s = nullptr;
   DBuf<int> v_off, e_off, f_off, vbody, ev, fv, scene_beg, scene_end;
   DBuf<double> rest, mass, Ic, rest_box, q, q0, dqdt, dq, X, Xq, X0, lastdq;
@@ -107,7 +108,7 @@ struct Engine {
 
   Geo geo() const {
     Geo g;
-    g.nb = nb; g.nv = nv; g.ne = ne; g.nf = nf;
+    g.nb = nb; g.nv = nv; g.ne = ne; g.nf = nf; g.max_prims = max_prims;
     g.v_off = v_off.p; g.e_off = e_off.p; g.f_off = f_off.p;
     g.rest = rest.p; g.vbody = vbody.p; g.ev = ev.p; g.fv = fv.p;
     g.mass = mass.p; g.Ic = Ic.p; g.rest_box = rest_box.p;
@@ -143,7 +144,9 @@ struct Engine {
     nbufs.pt_c.release(); nbufs.ee_c.release(); nbufs.pt_seg.release(); nbufs.ee_seg.release();
     nbufs.ovr.release(); nbufs.has.release(); nbufs.D.release(); nbufs.Dinv.release(); nbufs.grad.release();
     nbufs.x.release(); nbufs.r.release(); nbufs.z.release(); nbufs.p.release(); nbufs.qv.release();
-    nbufs.bpA.release(); nbufs.bpB.release(); nbufs.sc_rz.release(); nbufs.sc_bb.release();
+    nbufs.Hrow.release(); nbufs.rcol.release(); nbufs.rn.release();
+    nbufs.gpA.release(); nbufs.gpB.release(); nbufs.grp_body.release(); nbufs.grp_n.release();
+    nbufs.grp_scene.release(); nbufs.sc_gbeg.release(); nbufs.sc_gend.release(); nbufs.sc_rz.release(); nbufs.sc_bb.release();
     nbufs.sc_conv.release(); nbufs.sc_iters.release(); nbufs.n_active.release();
     nbufs.e_off.release(); nbufs.e_chunk_cnt.release(); nbufs.e_chunk_off.release(); nbufs.e_scan_tmp.release();
     nbufs.e_out.release(); nbufs.red.release(); nbufs.status.release();
@@ -214,6 +217,9 @@ struct Engine {
     std::vector<int> hvb(nv), hev(2 * (size_t)ne), hfv(3 * (size_t)nf), sb(nb), se(nb);
     std::vector<double> rb(6 * (size_t)nb);
     for (int b = 0; b < nb; ++b) {
+      int np = (d->vert_off[b + 1] - d->vert_off[b]) + (d->edge_off[b + 1] - d->edge_off[b]) +
+               (d->face_off[b + 1] - d->face_off[b]);
+      max_prims = np > max_prims ? np : max_prims;
       for (int v = d->vert_off[b]; v < d->vert_off[b + 1]; ++v) hvb[v] = b;
       for (int e = d->edge_off[b]; e < d->edge_off[b + 1]; ++e)
         for (int k = 0; k < 2; ++k) {
@@ -282,6 +288,7 @@ struct Engine {
     upload(bscene, hbs.data(), nb);
     upload(sc_beg, h_sc_beg.data(), ns);
     upload(sc_end, h_sc_end.data(), ns);
+    abd::pcg_groups(h_sc_beg, h_sc_end, nbufs, s);
     sc_on.ensure(ns);
     sc_alpha.ensure(ns);
     sc_factor.ensure(ns);

@@ -390,36 +390,66 @@ __global__ void k_block_inverse(int nb, const double* D, double* Dinv, int* stat
 }
 
 // ---------------------------------------------------------------------------------
-// Block-Jacobi PCG, one cooperative launch; slots (body, row) in groups of 16 lanes so
-// the 12 rows of a body always sit in one warp.
+// Block-Jacobi PCG, one cooperative launch.
+//
+// The system is first copied into row-block form (k_pcg_rows): for each body its diagonal
+// block, then every off-diagonal block that holds a contribution, each stored row-major
+// for that body's rows, so a row of the product reads 96 contiguous bytes per block and
+// empty overlaps cost nothing. A body's product is split over NPART groups of 16 lanes
+// (lane = row, rows 12..15 idle) that take every NPART-th block of the row list; the
+// partial rows are added in part order in shared memory.
+//
+// Bodies are handled in groups of up to GB consecutive bodies of one scene, cut from each
+// scene's first body (a scene of n bodies has ceil(n / GB) groups); a CTA takes one group
+// at a time, so every CTA works on one scene.
+//
+// One iteration is two grid-wide phases:
+//   A_k: stopping test and beta from the previous r.r and r.z; p_k = z + beta p_{k-1}
+//        applied to every neighbour read (p kept in two buffers by iteration parity, so no
+//        barrier is needed between the update and the product); q = H p_k; p.q.
+//   B_k: alpha = r.z / p.q; x += alpha p, r -= alpha q, z = M^-1 r; r.r, r.z.
 //
 // Every scene of a batch runs its own CG (its own alpha, beta and stopping test), so a
 // scene solved in a batch gets exactly the iterates it gets when solved alone. Dot
-// products are reduced per body (16-lane shuffle tree), then per scene over the scene's
-// bodies in a scene-relative order (thread t of a 256-thread block takes bodies
-// beg + t, beg + t + 256, ...), which does not depend on where the scene sits in the
-// batch. Every block that holds bodies of a scene computes that scene's sums itself
-// (no extra grid barrier); the block holding the scene's first body publishes the
-// scalars carried to the next iteration, in buffers alternating by iteration parity.
+// products are reduced per body (16-lane shuffle tree), per group (its bodies in order),
+// then per scene over the scene's groups (thread t takes groups gbeg + t, gbeg + t + NT,
+// ..., then a fixed tree); groups are cut relative to the scene's first body, so none of
+// this depends on where the scene sits in a batch. Every CTA working on a scene computes
+// the scene's sums itself; the CTA holding the scene's first group publishes the scalars
+// carried to the next iteration, in buffers alternating by iteration parity.
+constexpr int NPART = 4;                 // 16-lane groups per body in the product
+constexpr int BODY_SLOTS = 16 * NPART;   // threads per body
+constexpr int GB = 8;                    // bodies per group
+constexpr int PCG_NT = GB * BODY_SLOTS;  // threads per CTA
+
 struct PcgArgs {
-  int nb, ns;
-  const int *row_ptr, *col, *upidx, *has;
-  const double *ovr, *D, *Dinv, *b;
-  const int *bscene, *sc_beg, *sc_end;  // body -> scene; body range of each scene
+  int nb, ns, ngrp;
+  const int *row_ptr, *rcol, *rn;       // row-block lists: slot body + row_ptr[body], rn blocks
+  const double *Hrow, *Dinv, *b;
+  const int *grp_body, *grp_n, *grp_scene;  // group -> first body, bodies, scene
+  const int *sc_gbeg, *sc_gend;             // scene -> its groups
   const int* sc_on;                     // ns: 0 -> the scene is not solved (dq = 0)
-  double *x, *r, *z, *p, *q, *dq;
-  double *bpA, *bpB;                    // 2 nb per-body partial sums
+  double *x, *r, *z, *q, *dq;
+  double* pbuf;                         // 2 x 12 nb: search direction by iteration parity
+  double *gpA, *gpB;                    // 2 per group: partial sums
   double *sc_rz;                        // 2 ns (parity)
   double *sc_bb;                        // ns
   int *sc_conv;                         // 2 ns (parity)
   int *sc_iters;                        // ns
-  int *n_active;                        // 2 (parity)
+  int *n_active;                        // 3 (iteration mod 3)
   double tol2;
   int maxit;
   int* out;  // [0] status, [1] iterations (max over scenes)
 };
 
-__device__ __forceinline__ double row_spmv(const PcgArgs& a, int body, int row, const double* v) {
+// Assembled system as stored by the assembly (diagonal blocks D, off-diagonal blocks in
+// the per-overlap records), for products outside the PCG.
+struct SysView {
+  const int *row_ptr, *col, *upidx, *has;
+  const double *ovr, *D;
+};
+
+__device__ __forceinline__ double row_spmv(const SysView& a, int body, int row, const double* v) {
   double s = 0.0;
   const double* Db = a.D + 144 * body + 12 * row;
   const double* vb = v + 12 * body;
@@ -442,6 +472,85 @@ __device__ __forceinline__ double row_spmv(const PcgArgs& a, int body, int row, 
   return s;
 }
 
+// One warp per body: the diagonal block, then the off-diagonal blocks with a
+// contribution in overlap-list order, transposed where the body is the record's J side.
+// kept[0] accumulates the blocks kept (for the algorithmic byte count).
+__global__ void k_pcg_rows(int nb, const int* row_ptr, const int* col, const int* upidx, const int* has,
+                           const double* ovr, const double* D, double* Hrow, int* rcol, int* rn, int* kept) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nb) return;
+  const int body = warp;
+  const int base = body + row_ptr[body];
+  for (int t = lane; t < 144; t += 32) Hrow[(size_t)base * 144 + t] = D[(size_t)body * 144 + t];
+  if (lane == 0) rcol[base] = body;
+  int n = 1;
+  const unsigned below = (1u << lane) - 1u;
+  const int e1 = row_ptr[body + 1];
+  for (int e0 = row_ptr[body]; e0 < e1; e0 += 32) {
+    int e = e0 + lane;
+    int u = -1, cb = 0;
+    if (e < e1) {
+      u = upidx[e];
+      cb = col[e];
+      if (u >= 0 && !has[u]) u = -1;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, u >= 0);
+    if (u >= 0) rcol[base + n + __popc(m & below)] = cb;
+    while (m) {
+      int l = __ffs(m) - 1;
+      m &= m - 1;
+      int uu = __shfl_sync(0xffffffffu, u, l);
+      int cc = __shfl_sync(0xffffffffu, cb, l);
+      const double* B = ovr + (size_t)uu * CONTRIB + 288;
+      double* dst = Hrow + (size_t)(base + n) * 144;
+      for (int t = lane; t < 144; t += 32) {
+        int rr = t / 12, c = t - 12 * rr;
+        dst[t] = cc > body ? B[t] : B[12 * c + rr];
+      }
+      ++n;
+    }
+  }
+  if (lane == 0) {
+    rn[body] = n;
+    atomicAdd(kept, n);
+  }
+}
+
+// CTA-wide sums of v[2k], v[2k+1] over k in [beg, end) (thread t takes beg + t,
+// beg + t + NT, ..., then a shuffle tree and the warps in order); every thread gets them.
+__device__ __forceinline__ void cta_sum2(const double* v, int beg, int end, double& a, double& b, double* sh) {
+  double sa = 0.0, sb = 0.0;
+  for (int k = beg + (int)threadIdx.x; k < end; k += blockDim.x) {
+    sa += v[2 * k];
+    sb += v[2 * k + 1];
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sa += __shfl_xor_sync(0xffffffffu, sa, o);
+    sb += __shfl_xor_sync(0xffffffffu, sb, o);
+  }
+  if (lane == 0) {
+    sh[2 * w] = sa;
+    sh[2 * w + 1] = sb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0, tb = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+      ta += sh[2 * i];
+      tb += sh[2 * i + 1];
+    }
+    sh[64] = ta;
+    sh[65] = tb;
+  }
+  __syncthreads();
+  a = sh[64];
+  b = sh[65];
+  __syncthreads();
+}
+
+// Block-wide sums of a and b (shuffle tree, then the warps in order); thread 0 gets them.
 __device__ __forceinline__ void block_sum2(double& a, double& b, double* sh) {
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -465,25 +574,6 @@ __device__ __forceinline__ void block_sum2(double& a, double& b, double* sh) {
   }
 }
 
-// Block-wide sums of v[2k], v[2k+1] over bodies k in [beg, end), in the scene-relative
-// order described above; the result is broadcast to every thread of the block.
-__device__ __forceinline__ void scene_sum2(const double* v, int beg, int end, double& a, double& b, double* sh) {
-  double sa = 0.0, sb = 0.0;
-  for (int k = beg + (int)threadIdx.x; k < end; k += blockDim.x) {
-    sa += v[2 * k];
-    sb += v[2 * k + 1];
-  }
-  block_sum2(sa, sb, sh);
-  if (threadIdx.x == 0) {
-    sh[64] = sa;
-    sh[65] = sb;
-  }
-  __syncthreads();
-  a = sh[64];
-  b = sh[65];
-  __syncthreads();
-}
-
 // Sum over the 16 lanes of a body's slot group (rows 12..15 contribute 0).
 __device__ __forceinline__ double body_sum16(double v) {
 #pragma unroll
@@ -491,39 +581,69 @@ __device__ __forceinline__ double body_sum16(double v) {
   return v;
 }
 
+// Group partials: the bodies' (c0, c1) in order, written by thread 0 to gp[2 g].
+__device__ __forceinline__ void group_sum2(double c0, double c1, bool lead, int lb, int nbody, double* s_bp,
+                                          double* gp, int g) {
+  if (lead) {
+    s_bp[2 * lb] = c0;
+    s_bp[2 * lb + 1] = c1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && g >= 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int i = 0; i < nbody; ++i) {
+      t0 += s_bp[2 * i];
+      t1 += s_bp[2 * i + 1];
+    }
+    gp[2 * g] = t0;
+    gp[2 * g + 1] = t1;
+  }
+}
+
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
 
-__global__ void __launch_bounds__(256) k_pcg(PcgArgs a) {
+// p_k entry: z + beta p_{k-1} (one expression for a body's own entry and for every read
+// of it as a neighbour, so all readers see one value)
+__device__ __forceinline__ double dir(double z, double beta, double p) { return __fma_rn(beta, p, z); }
+
+__global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
   cg::grid_group grid = cg::this_grid();
   __shared__ double sh[80];
-  __shared__ double s_val[16];   // per scene of the current body group: alpha or beta
-  __shared__ int s_flag[16];     // per scene of the current body group: converged now
-  const int nslot = a.nb * 16;
-  const int nthr = gridDim.x * blockDim.x;
-  const int nloop = (nslot + nthr - 1) / nthr;
+  __shared__ double s_part[PCG_NT];
+  __shared__ double s_bp[2 * GB];
+  __shared__ __align__(16) double s_v[PCG_NT / 16][12];  // direction entries of the block being read
+  __shared__ double s_val;   // alpha or beta of this CTA's scene
+  __shared__ int s_flag;     // 1: this CTA's scene does no work in this phase
+  const int nloop = (a.ngrp + gridDim.x - 1) / gridDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int part = (threadIdx.x >> 4) & (NPART - 1), row = threadIdx.x & 15;
+  const int lb = threadIdx.x / BODY_SLOTS;   // body of the group
+  const int hg = threadIdx.x >> 4;           // 16-lane group of the CTA
+  const bool lead = part == 0 && row == 0;   // holds its body's partial sums
 
-  // scenes [s_lo, s_hi] of the 16-body group this block handles in loop step `it`
-  auto group = [&](int it, int& b0, int& s_lo, int& s_hi) {
-    b0 = (blockIdx.x * blockDim.x + it * nthr) >> 4;
-    if (b0 >= a.nb) {
-      s_lo = 0;
-      s_hi = -1;
+  // group handled in loop step `it`: g (or -1), its scene, this thread's body (or -1)
+  auto group = [&](int it, int& g, int& sc, int& body, int& nbody) {
+    g = blockIdx.x + it * gridDim.x;
+    if (g >= a.ngrp) {
+      g = -1;
+      sc = -1;
+      body = -1;
+      nbody = 0;
       return;
     }
-    int b1 = b0 + 15 < a.nb ? b0 + 15 : a.nb - 1;
-    s_lo = a.bscene[b0];
-    s_hi = a.bscene[b1];
+    sc = a.grp_scene[g];
+    nbody = a.grp_n[g];
+    body = lb < nbody ? a.grp_body[g] + lb : -1;
   };
 
-  // ---- init: x = 0, r = b, z = M^-1 b, p = z (zero for scenes not solved) ----
+  // ---- init: x = 0, r = b, z = M^-1 b, p_{-1} = 0 (zero for scenes not solved) ----
   for (int it = 0; it < nloop; ++it) {
-    int s = tid + it * nthr;
-    int body = s >> 4, row = s & 15;
+    int g, sc, body, nbody;
+    group(it, g, sc, body, nbody);
     double c0 = 0.0, c1 = 0.0;
-    if (s < nslot && row < 12) {
+    if (body >= 0 && part == 0 && row < 12) {
       int idx = 12 * body + row;
-      bool on = a.sc_on[a.bscene[body]] != 0;
+      bool on = a.sc_on[sc] != 0;
       double bv = on ? a.b[idx] : 0.0;
       double zv = 0.0;
       if (on) {
@@ -534,86 +654,139 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs a) {
       a.x[idx] = 0.0;
       a.r[idx] = bv;
       a.z[idx] = zv;
-      a.p[idx] = zv;
-      c0 = bv * zv;
-      c1 = bv * bv;
+      a.pbuf[idx] = 0.0;
+      a.pbuf[12 * a.nb + idx] = 0.0;
+      c0 = bv * bv;
+      c1 = bv * zv;
     }
     c0 = body_sum16(c0);
     c1 = body_sum16(c1);
-    if (s < nslot && row == 0) {
-      a.bpA[2 * body] = c0;
-      a.bpA[2 * body + 1] = c1;
-    }
+    group_sum2(c0, c1, lead && body >= 0, lb, nbody, s_bp, a.gpB, g);
+    __syncthreads();
+  }
+  if (tid == 0) {
+    a.n_active[0] = 0;
+    a.n_active[1] = 0;
+    a.n_active[2] = 0;
   }
   grid.sync();
-  for (int it = 0; it < nloop; ++it) {
-    int b0, s_lo, s_hi;
-    group(it, b0, s_lo, s_hi);
-    for (int sc = s_lo; sc <= s_hi; ++sc) {
-      if (a.sc_beg[sc] < b0) continue;  // published by the group holding the scene's first body
-      double rz, bb;
-      scene_sum2(a.bpA, a.sc_beg[sc], a.sc_end[sc], rz, bb, sh);
-      if (threadIdx.x == 0) {
-        bool conv = !a.sc_on[sc] || bb == 0.0;
-        a.sc_rz[sc] = rz;
-        a.sc_bb[sc] = bb;
-        a.sc_conv[sc] = conv ? 1 : 0;
-        a.sc_iters[sc] = 0;
-        if (!conv) atomicAdd(&a.n_active[0], 1);
-      }
-    }
-  }
-  grid.sync();
-  int nact = ld_volatile(&a.n_active[0]);
   int k = 0;
-  for (; k < a.maxit && nact > 0; ++k) {
-    const int par = k & 1, nxt = par ^ 1;
-    const double* rz_cur = a.sc_rz + par * a.ns;
-    double* rz_nxt = a.sc_rz + nxt * a.ns;
-    const int* conv_cur = a.sc_conv + par * a.ns;
-    int* conv_nxt = a.sc_conv + nxt * a.ns;
-    if (tid == 0) a.n_active[nxt] = 0;
-    // ---- A: q = H p, per-body p.q ----
+  for (;; ++k) {
+    const int par = k & 1;
+    const double* p_old = a.pbuf + (par ^ 1) * 12 * a.nb;  // p_{k-1}
+    double* p_new = a.pbuf + par * 12 * a.nb;               // p_k
+    double* rz_cur = a.sc_rz + par * a.ns;
+    const double* rz_prev = a.sc_rz + (par ^ 1) * a.ns;
+    int* conv_cur = a.sc_conv + par * a.ns;
+    const int* conv_prev = a.sc_conv + (par ^ 1) * a.ns;
+    if (tid == 0) a.n_active[(k + 1) % 3] = 0;
+    // ---- A_k: stopping test, beta, q = H p_k, p.q ----
     for (int it = 0; it < nloop; ++it) {
-      int s = tid + it * nthr;
-      int body = s >> 4, row = s & 15;
-      double c0 = 0.0;
-      if (s < nslot && row < 12 && !conv_cur[a.bscene[body]]) {
-        int idx = 12 * body + row;
-        double qv = row_spmv(a, body, row, a.p);
-        a.q[idx] = qv;
-        c0 = a.p[idx] * qv;
-      }
-      c0 = body_sum16(c0);
-      if (s < nslot && row == 0) {
-        a.bpA[2 * body] = c0;
-        a.bpA[2 * body + 1] = 0.0;
-      }
-    }
-    grid.sync();
-    // ---- B: alpha per scene; x += alpha p, r -= alpha q, z = M^-1 r; per-body r.r, r.z ----
-    for (int it = 0; it < nloop; ++it) {
-      int b0, s_lo, s_hi;
-      group(it, b0, s_lo, s_hi);
-      for (int sc = s_lo; sc <= s_hi; ++sc) {
-        if (conv_cur[sc]) continue;
-        double pq, dummy;
-        scene_sum2(a.bpA, a.sc_beg[sc], a.sc_end[sc], pq, dummy, sh);
-        if (threadIdx.x == 0) s_val[sc - s_lo] = rz_cur[sc] / pq;
+      int g, sc, body, nbody;
+      group(it, g, sc, body, nbody);
+      if (g >= 0) {
+        const bool owner = g == a.sc_gbeg[sc];
+        if (k > 0 && conv_prev[sc]) {
+          if (threadIdx.x == 0) {
+            if (owner) conv_cur[sc] = 1;
+            s_flag = 1;
+          }
+        } else {
+          double rr, rz;
+          cta_sum2(a.gpB, a.sc_gbeg[sc], a.sc_gend[sc], rr, rz, sh);
+          if (threadIdx.x == 0) {
+            bool conv;
+            if (k == 0) {
+              conv = !a.sc_on[sc] || rr == 0.0;
+              if (owner) a.sc_bb[sc] = rr;
+            } else {
+              conv = !(rr > a.tol2 * a.sc_bb[sc]);
+            }
+            s_val = k == 0 ? 0.0 : rz / rz_prev[sc];
+            s_flag = conv || k == a.maxit;
+            if (owner) {
+              rz_cur[sc] = rz;
+              conv_cur[sc] = conv ? 1 : 0;
+              if (conv) {
+                a.sc_iters[sc] = k;
+              } else if (k == a.maxit) {
+                a.sc_iters[sc] = k;
+                a.out[0] = ABD_ERR_PCG_NOCONV;
+              } else {
+                atomicAdd(&a.n_active[k % 3], 1);
+              }
+            }
+          }
+        }
       }
       __syncthreads();
-      int s = tid + it * nthr;
-      int body = s >> 4, row = s & 15;
-      bool act = s < nslot && row < 12 && !conv_cur[a.bscene[body]];
-      int idx = 12 * body + row;
+      const bool act = g >= 0 && !s_flag;
+      const double beta = act ? s_val : 0.0;
+      double acc = 0.0;
+      if (act && body >= 0) {
+        // the two 16-lane halves of a warp are different parts and may run different
+        // trip counts: each half synchronises only itself
+        const unsigned half = 0xffffu << (threadIdx.x & 16);
+        const int base = body + a.row_ptr[body], n = a.rn[body];
+        for (int j = part; j < n; j += NPART) {
+          const int cb = a.rcol[base + j];
+          if (row < 12) s_v[hg][row] = dir(a.z[12 * cb + row], beta, p_old[12 * cb + row]);
+          __syncwarp(half);
+          if (row < 12) {
+            const double2* H = reinterpret_cast<const double2*>(a.Hrow + (size_t)(base + j) * 144 + 12 * row);
+            const double2* v = reinterpret_cast<const double2*>(s_v[hg]);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+              double2 h = H[c], vv = v[c];
+              acc += h.x * vv.x;
+              acc += h.y * vv.y;
+            }
+          }
+          __syncwarp(half);
+        }
+      }
+      s_part[threadIdx.x] = acc;
+      __syncthreads();
+      double c0 = 0.0;
+      if (act && body >= 0 && part == 0 && row < 12) {
+        const double* sp = s_part + lb * BODY_SLOTS + row;
+        double qv = sp[0];
+#pragma unroll
+        for (int pp = 1; pp < NPART; ++pp) qv += sp[16 * pp];
+        int idx = 12 * body + row;
+        double pv = dir(a.z[idx], beta, p_old[idx]);
+        p_new[idx] = pv;
+        a.q[idx] = qv;
+        c0 = pv * qv;
+      }
+      c0 = body_sum16(c0);
+      if (act) group_sum2(c0, 0.0, lead && body >= 0, lb, nbody, s_bp, a.gpA, g);
+      __syncthreads();
+    }
+    if (k == a.maxit) break;
+    grid.sync();
+    if (ld_volatile(&a.n_active[k % 3]) == 0) break;
+    // ---- B_k: alpha; x += alpha p, r -= alpha q, z = M^-1 r; r.r, r.z ----
+    for (int it = 0; it < nloop; ++it) {
+      int g, sc, body, nbody;
+      group(it, g, sc, body, nbody);
+      const bool act = g >= 0 && !conv_cur[sc];
       if (act) {
-        double alpha = s_val[a.bscene[body] - s_lo];
-        a.x[idx] += alpha * a.p[idx];
+        double pq, dummy;
+        cta_sum2(a.gpA, a.sc_gbeg[sc], a.sc_gend[sc], pq, dummy, sh);
+        if (threadIdx.x == 0) s_val = rz_cur[sc] / pq;
+      }
+      __syncthreads();
+      const bool mine = act && body >= 0 && part == 0 && row < 12;
+      const int idx = 12 * body + row;
+      if (mine) {
+        double alpha = s_val;
+        a.x[idx] += alpha * p_new[idx];
         a.r[idx] -= alpha * a.q[idx];
       }
       __syncwarp();
       double c0 = 0.0, c1 = 0.0;
-      if (act) {
+      if (mine) {
         const double* Mi = a.Dinv + 144 * body + 12 * row;
         double zv = 0;
 #pragma unroll
@@ -625,66 +798,18 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs a) {
       }
       c0 = body_sum16(c0);
       c1 = body_sum16(c1);
-      if (s < nslot && row == 0) {
-        a.bpB[2 * body] = c0;
-        a.bpB[2 * body + 1] = c1;
-      }
+      if (act) group_sum2(c0, c1, lead && body >= 0, lb, nbody, s_bp, a.gpB, g);
       __syncthreads();
     }
     grid.sync();
-    // ---- C: stopping test and beta per scene; p = z + beta p ----
-    for (int it = 0; it < nloop; ++it) {
-      int b0, s_lo, s_hi;
-      group(it, b0, s_lo, s_hi);
-      for (int sc = s_lo; sc <= s_hi; ++sc) {
-        bool owner = a.sc_beg[sc] >= b0;
-        if (conv_cur[sc]) {
-          if (owner && threadIdx.x == 0) conv_nxt[sc] = 1;
-          continue;
-        }
-        double rr, rzn;
-        scene_sum2(a.bpB, a.sc_beg[sc], a.sc_end[sc], rr, rzn, sh);
-        if (threadIdx.x == 0) {
-          bool conv = !(rr > a.tol2 * a.sc_bb[sc]);
-          s_val[sc - s_lo] = rzn / rz_cur[sc];
-          s_flag[sc - s_lo] = conv ? 1 : 0;
-          if (owner) {
-            rz_nxt[sc] = rzn;
-            conv_nxt[sc] = conv ? 1 : 0;
-            if (conv) a.sc_iters[sc] = k + 1;
-            else atomicAdd(&a.n_active[nxt], 1);
-          }
-        }
-      }
-      __syncthreads();
-      int s = tid + it * nthr;
-      int body = s >> 4, row = s & 15;
-      if (s < nslot && row < 12) {
-        int sc = a.bscene[body];
-        if (!conv_cur[sc] && !s_flag[sc - s_lo]) {
-          int idx = 12 * body + row;
-          a.p[idx] = a.z[idx] + s_val[sc - s_lo] * a.p[idx];
-        }
-      }
-      __syncthreads();
-    }
-    grid.sync();
-    nact = ld_volatile(&a.n_active[nxt]);
   }
-  // dq = -x
+  // dq = -x (each entry written by the thread that owns it)
   for (int it = 0; it < nloop; ++it) {
-    int s = tid + it * nthr;
-    int body = s >> 4, row = s & 15;
-    if (s < nslot && row < 12) a.dq[12 * body + row] = -a.x[12 * body + row];
+    int g, sc, body, nbody;
+    group(it, g, sc, body, nbody);
+    if (body >= 0 && part == 0 && row < 12) a.dq[12 * body + row] = -a.x[12 * body + row];
   }
-  if (tid == 0) {
-    a.out[1] = k;
-    if (nact > 0) a.out[0] = ABD_ERR_PCG_NOCONV;
-  }
-  // scenes still running at the iteration cap
-  if (nact > 0)
-    for (int sc = tid; sc < a.ns; sc += nthr)
-      if (!a.sc_conv[(k & 1) * a.ns + sc]) a.sc_iters[sc] = k;
+  if (tid == 0) a.out[1] = k;
 }
 
 // ---------------------------------------------------------------------------------
@@ -1009,13 +1134,7 @@ __global__ void k_spmv(int nb, const int* row_ptr, const int* col, const int* up
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   int body = s >> 4, row = s & 15;
   if (body >= nb || row >= 12) return;
-  PcgArgs a;
-  a.row_ptr = row_ptr;
-  a.col = col;
-  a.upidx = upidx;
-  a.has = has;
-  a.ovr = ovr;
-  a.D = D;
+  SysView a{row_ptr, col, upidx, has, ovr, D};
   y[12 * body + row] = row_spmv(a, body, row, x);
 }
 
@@ -1087,67 +1206,101 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   B.x.ensure(12 * (size_t)nb);
   B.r.ensure(12 * (size_t)nb);
   B.z.ensure(12 * (size_t)nb);
-  B.p.ensure(12 * (size_t)nb);
+  B.p.ensure(24 * (size_t)nb);
   B.qv.ensure(12 * (size_t)nb);
-  B.bpA.ensure(2 * (size_t)nb);
-  B.bpB.ensure(2 * (size_t)nb);
+  B.Hrow.ensure(144 * ((size_t)nb + S.nnz));
+  B.rcol.ensure((size_t)nb + S.nnz);
+  B.rn.ensure(nb);
+  if (B.ngrp <= 0) {  // pcg_groups was not called for these scenes
+    *status = ABD_ERR_INVALID;
+    return 0;
+  }
+  B.gpA.ensure(2 * (size_t)B.ngrp);
+  B.gpB.ensure(2 * (size_t)B.ngrp);
   B.sc_rz.ensure(2 * (size_t)ns);
   B.sc_bb.ensure(ns);
   B.sc_conv.ensure(2 * (size_t)ns);
   B.sc_iters.ensure(ns);
-  B.n_active.ensure(2);
-  CK(cudaMemsetAsync(B.n_active.p, 0, 2 * sizeof(int), s));
+  B.n_active.ensure(3);
+  // solve setup (counted with the preconditioner): row-block copy of the system
+  KLAUNCH(K_BLOCK_INVERSE, s, k_pcg_rows<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(nb, S.row_ptr.p, S.col.p,
+                                                                                        S.upidx.p, B.has.p, B.ovr.p,
+                                                                                        B.D.p, B.Hrow.p, B.rcol.p,
+                                                                                        B.rn.p, B.status.p + 2));
   static int max_blocks = 0;
   if (!max_blocks) {
     int dev, sms, per;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg, 256, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg, PCG_NT, 0));
     max_blocks = sms * (per > 0 ? per : 1);
   }
-  int want = nblk((long long)nb * 16, 256);
-  int grid = want < max_blocks ? want : max_blocks;
+  int grid = B.ngrp < max_blocks ? B.ngrp : max_blocks;
   if (grid < 1) grid = 1;
   PcgArgs a;
   a.nb = nb;
   a.ns = ns;
+  a.ngrp = B.ngrp;
   a.row_ptr = S.row_ptr.p;
-  a.col = S.col.p;
-  a.upidx = S.upidx.p;
-  a.has = B.has.p;
-  a.ovr = B.ovr.p;
-  a.D = B.D.p;
+  a.rcol = B.rcol.p;
+  a.rn = B.rn.p;
+  a.Hrow = B.Hrow.p;
   a.Dinv = B.Dinv.p;
   a.b = B.grad.p;
-  a.bscene = g.bscene;
-  a.sc_beg = g.sc_beg;
-  a.sc_end = g.sc_end;
+  a.grp_body = B.grp_body.p;
+  a.grp_n = B.grp_n.p;
+  a.grp_scene = B.grp_scene.p;
+  a.sc_gbeg = B.sc_gbeg.p;
+  a.sc_gend = B.sc_gend.p;
   a.sc_on = sc_on;
   a.x = B.x.p;
   a.r = B.r.p;
   a.z = B.z.p;
-  a.p = B.p.p;
+  a.pbuf = B.p.p;
   a.q = B.qv.p;
   a.dq = dq;
-  a.bpA = B.bpA.p;
-  a.bpB = B.bpB.p;
+  a.gpA = B.gpA.p;
+  a.gpB = B.gpB.p;
   a.sc_rz = B.sc_rz.p;
   a.sc_bb = B.sc_bb.p;
   a.sc_conv = B.sc_conv.p;
   a.sc_iters = B.sc_iters.p;
   a.n_active = B.n_active.p;
   a.tol2 = rel_tol * rel_tol;
-  a.maxit = max_iter;
+  a.maxit = max_iter < 0 ? 0 : max_iter;
   a.out = B.status.p;
   void* args[] = {&a};
-  KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel((void*)k_pcg, dim3(grid), dim3(256), args, 0, s)));
-  CK(cudaMemcpyAsync(B.h_int, B.status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel((void*)k_pcg, dim3(grid), dim3(PCG_NT), args, 0, s)));
+  CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
   if (scene_iters) CK(cudaMemcpyAsync(scene_iters, B.sc_iters.p, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   *status = B.h_int[0];
-  // per iteration: the block matrix once (1152 B per block) and ~6 vector streams
-  prof_work(K_PCG, B.h_int[1], B.h_int[1] * (1152.0 * (nb + 2.0 * S.nov) + 6 * 96.0 * nb) + 1152.0 * nb);
+  // per iteration: the kept blocks once (1152 B each) and ~6 vector streams
+  prof_work(K_PCG, B.h_int[1], B.h_int[1] * (1152.0 * B.h_int[2] + 6 * 96.0 * nb) + 1152.0 * nb);
+  prof_work(K_BLOCK_INVERSE, 1, 2 * 1152.0 * B.h_int[2]);
   return B.h_int[1];
+}
+
+void pcg_groups(const std::vector<int>& sc_beg, const std::vector<int>& sc_end, NewtonBufs& B, cudaStream_t s) {
+  std::vector<int> gb, gn, gs, sgb, sge;
+  for (size_t k = 0; k < sc_beg.size(); ++k) {
+    sgb.push_back((int)gb.size());
+    for (int b = sc_beg[k]; b < sc_end[k]; b += GB) {
+      gb.push_back(b);
+      gn.push_back(sc_end[k] - b < GB ? sc_end[k] - b : GB);
+      gs.push_back((int)k);
+    }
+    sge.push_back((int)gb.size());
+  }
+  B.ngrp = (int)gb.size();
+  DBuf<int>* dst[] = {&B.grp_body, &B.grp_n, &B.grp_scene, &B.sc_gbeg, &B.sc_gend};
+  std::vector<int>* src[] = {&gb, &gn, &gs, &sgb, &sge};
+  for (int i = 0; i < 5; ++i) {
+    dst[i]->ensure(src[i]->size() + 1);
+    if (!src[i]->empty())
+      CK(cudaMemcpyAsync(dst[i]->p, src[i]->data(), src[i]->size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaStreamSynchronize(s));
 }
 
 void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_bi, NewtonBufs& B,
