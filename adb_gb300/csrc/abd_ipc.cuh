@@ -224,8 +224,12 @@ DEV void psd_project(double (&S)[N][N]) {
 }
 
 // Eigen-projection of a small symmetric matrix held in registers (fully unrolled
-// cyclic Jacobi; N <= 5). Returns whether any eigenvalue was negative (then S holds the
-// projection), leaving S untouched otherwise.
+// cyclic Jacobi on the upper triangle; N <= 5). Returns whether any eigenvalue was
+// negative (then S holds the projection), leaving S untouched otherwise.
+// A rotation annihilating a_pq uses t = sgn(h) a_pq / (|h| + sqrt(h^2 + a_pq^2)) with
+// h = (a_qq - a_pp) / 2, c = 1 / sqrt(1 + t^2), s = t c, and updates the 2x2 block in
+// closed form (a_pp -= t a_pq, a_qq += t a_pq, a_pq = 0): one division and two
+// square-root evaluations per rotation, and only the entries of one triangle.
 template <int N>
 DEV bool psd_project_small(double (&S)[N][N]) {
   double A[N][N], V[N][N];
@@ -237,36 +241,36 @@ DEV bool psd_project_small(double (&S)[N][N]) {
       V[i][j] = (i == j) ? 1.0 : 0.0;
     }
   for (int sweep = 0; sweep < 20; ++sweep) {
-    double off = 0, tot = 0;
+    double off = 0, dg = 0;
 #pragma unroll
-    for (int i = 0; i < N; ++i)
+    for (int i = 0; i < N; ++i) {
+      dg += A[i][i] * A[i][i];
 #pragma unroll
-      for (int j = 0; j < N; ++j) {
-        double v = A[i][j] * A[i][j];
-        tot += v;
-        if (i != j) off += v;
-      }
-    if (off <= 1e-32 * tot || off == 0.0) break;
+      for (int j = i + 1; j < N; ++j) off += A[i][j] * A[i][j];
+    }
+    if (off == 0.0 || 2 * off <= 1e-32 * (dg + 2 * off)) break;
 #pragma unroll
     for (int p = 0; p < N - 1; ++p)
 #pragma unroll
       for (int q = p + 1; q < N; ++q) {
         double apq = A[p][q];
-        if (apq != 0.0) {
-          double theta = (A[q][q] - A[p][p]) / (2 * apq);
-          double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
-          double c = 1 / sqrt(t * t + 1), s = t * c;
+        double h = 0.5 * (A[q][q] - A[p][p]);
+        double den = apq != 0.0 ? fabs(h) + sqrt(h * h + apq * apq) : 0.0;
+        if (den > 0.0) {
+          double t = (h >= 0 ? apq : -apq) / den;
+          double c = rsqrt(1.0 + t * t), s = t * c;
+          A[p][p] -= t * apq;
+          A[q][q] += t * apq;
 #pragma unroll
           for (int k = 0; k < N; ++k) {
-            double akp = A[k][p], akq = A[k][q];
-            A[k][p] = c * akp - s * akq;
-            A[k][q] = s * akp + c * akq;
-          }
-#pragma unroll
-          for (int k = 0; k < N; ++k) {
-            double apk = A[p][k], aqk = A[q][k];
-            A[p][k] = c * apk - s * aqk;
-            A[q][k] = s * apk + c * aqk;
+            if (k == p || k == q) continue;
+            double akp = k < p ? A[k][p] : A[p][k];
+            double akq = k < q ? A[k][q] : A[q][k];
+            double np_ = c * akp - s * akq, nq = s * akp + c * akq;
+            if (k < p) A[k][p] = np_;
+            else A[p][k] = np_;
+            if (k < q) A[k][q] = nq;
+            else A[q][k] = nq;
           }
 #pragma unroll
           for (int k = 0; k < N; ++k) {
@@ -274,9 +278,8 @@ DEV bool psd_project_small(double (&S)[N][N]) {
             V[k][p] = c * vkp - s * vkq;
             V[k][q] = s * vkp + c * vkq;
           }
-          A[p][q] = 0.0;
-          A[q][p] = 0.0;
         }
+        A[p][q] = 0.0;
       }
   }
   bool neg = false;

@@ -24,10 +24,51 @@ inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 // ---------------------------------------------------------------------------------
 // Per-pair terms. kind 0: PT (point on body A, triangle on body B); 1: EE.
+// Stencil class of a pair (parameters of its closest-point problem, m = 0, 1, 2): the
+// size of the projection `pair_reduced` runs. PT: vertex-vertex 0-2, vertex-edge 3-5,
+// face 6; EE: vertex-vertex 0-3, vertex-edge 4-7, edge-edge 8.
+__device__ __forceinline__ int stencil_class(int kind, int ty) {
+  return kind == 0 ? (ty <= 2 ? 0 : (ty <= 5 ? 1 : 2)) : (ty <= 3 ? 0 : (ty <= 7 ? 1 : 2));
+}
+constexpr int CLS_T = 256;
+
+// Pairs per stencil class in each block of CLS_T pairs: cnt[c * nblk + block].
+__global__ void k_class_count(int kind, int n, const int8_t* ty, int* cnt) {
+  __shared__ int sc[3];
+  if (threadIdx.x < 3) sc[threadIdx.x] = 0;
+  __syncthreads();
+  int p = blockIdx.x * CLS_T + threadIdx.x;
+  if (p < n) atomicAdd(&sc[stencil_class(kind, ty[p])], 1);
+  __syncthreads();
+  if (threadIdx.x < 3) cnt[threadIdx.x * gridDim.x + blockIdx.x] = sc[threadIdx.x];
+}
+
+// Stable partition of the pairs by stencil class (offsets from the scan of k_class_count),
+// so that the warps of k_pair_terms run a single projection size.
+__global__ void k_class_scatter(int kind, int n, const int8_t* ty, const int* off, int* perm) {
+  __shared__ int wc[3][CLS_T / 32];
+  const int p = blockIdx.x * CLS_T + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int c = p < n ? stencil_class(kind, ty[p]) : -1;
+  unsigned m[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    m[k] = __ballot_sync(0xffffffffu, c == k);
+    if (lane == 0) wc[k][w] = __popc(m[k]);
+  }
+  __syncthreads();
+  if (c >= 0) {
+    int r = off[c * gridDim.x + blockIdx.x] + __popc(m[c] & ((1u << lane) - 1u));
+    for (int i = 0; i < w; ++i) r += wc[c][i];
+    perm[r] = p;
+  }
+}
+
 __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, int n, const int* tup,
-                                                    const int* pov, const int* ovI, double* C, double* lag) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
+                                                    const int* pov, const int* ovI, double* C, double* lag,
+                                                    const int* perm) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int p = perm[t];
   int A = tup[4 * p], a = tup[4 * p + 1], B = tup[4 * p + 2], b = tup[4 * p + 3];
   if (!scene_on(g, A)) return;  // scene not iterating: its blocks are not used
   int vid[4];
@@ -1180,11 +1221,21 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
   prof_work(K_PAIR_TERMS, (double)npt + nee, 412.0 * ((double)npt + nee));
   prof_work(K_OV_REDUCE, nov, 2.0 * 1152 * nov);
   prof_work(K_BODY_SYSTEM, nb, 2.0 * 1152 * nb + 2 * 96.0 * nb);
-  if (npt) {
-    KLAUNCH(K_PAIR_TERMS, s, k_pair_terms<<<nblk(npt, 128), 128, 0, s>>>(g, P, 0, npt, S.pt.p, S.pt_ov.p, S.ovI.p, B.pt_c.p, S.pt_lag.p));
-  }
-  if (nee) {
-    KLAUNCH(K_PAIR_TERMS, s, k_pair_terms<<<nblk(nee, 128), 128, 0, s>>>(g, P, 1, nee, S.ee.p, S.ee_ov.p, S.ovI.p, B.ee_c.p, S.ee_lag.p));
+  for (int kind = 0; kind < 2; ++kind) {
+    int n = kind ? nee : npt;
+    if (!n) continue;
+    int nb_c = nblk(n, CLS_T);
+    B.cls_cnt.ensure(3 * (size_t)nb_c);
+    B.cls_off.ensure(3 * (size_t)nb_c);
+    B.perm.ensure(n);
+    const int8_t* ty = kind ? S.ee_ty.p : S.pt_ty.p;
+    KLAUNCH(K_SEG, s, k_class_count<<<nb_c, CLS_T, 0, s>>>(kind, n, ty, B.cls_cnt.p));
+    scan_exclusive_int(B.cls_cnt.p, B.cls_off.p, 3 * nb_c, nullptr, s, B.cls_tmp);
+    KLAUNCH(K_SEG, s, k_class_scatter<<<nb_c, CLS_T, 0, s>>>(kind, n, ty, B.cls_off.p, B.perm.p));
+    KLAUNCH(K_PAIR_TERMS, s, k_pair_terms<<<nblk(n, 128), 128, 0, s>>>(g, P, kind, n, kind ? S.ee.p : S.pt.p,
+                                                                     kind ? S.ee_ov.p : S.pt_ov.p, S.ovI.p,
+                                                                     kind ? B.ee_c.p : B.pt_c.p,
+                                                                     kind ? S.ee_lag.p : S.pt_lag.p, B.perm.p));
   }
   if (nov) {
     KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, npt, S.pt_ov.p, B.pt_seg.p));

@@ -110,12 +110,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_unit(kernel):
-    """DRAM bytes per work unit of `kernel` from the committed ncu summary, if any."""
+def ncu_per_unit(kernel, key="traffic_per_unit"):
+    """A per-work-unit figure of `kernel` from the committed ncu summary, if any: DRAM
+    bytes (`traffic_per_unit`) or executed FP64 flops (`fp64_flops_per_unit`)."""
     if not os.path.exists(PROFILE_TRAFFIC):
         return None
     for line in open(PROFILE_TRAFFIC):
-        if line.startswith("traffic_per_unit") and kernel in line:
+        if line.startswith(key) and line.split("=")[0].split()[-1] == kernel:
             try:
                 return float(line.split("=")[1].split()[0])
             except Exception:
@@ -330,9 +331,18 @@ def run_gb300(args):
     avg_ms = d["ms"] / max(d["launches"], 1)
     bytes_per_launch = d["bytes"] / max(d["launches"], 1)
     achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
-    tpu = ncu_traffic_per_unit(dom)
+    tpu = ncu_per_unit(dom)
     traffic = tpu * d["units"] / max(d["launches"], 1) if tpu else None
     fp64_peak = measure_fp64_gflops()
+    # the dominant kernels of this FP64 path are bound by FP64 issue, not by HBM: their
+    # FP64 rate (flops per unit from one ncu capture x units per launch / live launch
+    # time) against the measured FP64 FMA peak
+    fpu = ncu_per_unit(dom, "fp64_flops_per_unit")
+    fp64_roof = None
+    if fpu and avg_ms > 0:
+        gf = fpu * d["units"] / max(d["launches"], 1) / (avg_ms * 1e-3) / 1e9
+        fp64_roof = {"achieved_gflops": gf, "peak_gflops": fp64_peak, "frac": gf / fp64_peak,
+                     "flops_per_unit": fpu, "source": "executed DFMA x2 + DADD + DMUL per unit (ncu), live time"}
 
     if rank == 0:
         line = {
@@ -351,7 +361,7 @@ def run_gb300(args):
                          "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                          "traffic": traffic, "avg_launch_ms": avg_ms, "launches": d["launches"],
                          "share": d["ms"] / tot if tot else None},
-            "fp64": {"peak_gflops_measured": fp64_peak},
+            "fp64": {"peak_gflops_measured": fp64_peak, "dominant_kernel": fp64_roof},
             "frame_stats": {"newton_iters": st.newton_iters, "ls_trials": st.ls_trials, "pcg_iters": st.pcg_iters,
                             "max_pt": st.n_pt, "max_ee": st.n_ee, "max_vg": st.n_vg,
                             "algorithmic_GB": st.bytes_moved / 1e9},
