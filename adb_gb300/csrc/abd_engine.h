@@ -220,7 +220,8 @@ enum { CONTRIB = 456 };  // dI(144) dJ(144) off(144) gI(12) gJ(12)
 struct NewtonBufs {
   DBuf<double> pt_c, ee_c;   // CONTRIB per pair (SoA)
   DBuf<int> pt_seg, ee_seg;  // nov + 1
-  DBuf<int> perm, cls_cnt, cls_off, cls_tmp;  // pairs in stencil-class order
+  DBuf<int> perm, cls_cnt, cls_off, cls_tmp;  // pairs in distance-type order
+  DBuf<double> prec;         // per-pair reduced Hessian records between the pair-term kernels
   DBuf<double> ovr;          // nov * CONTRIB
   DBuf<int> has;             // nov
   DBuf<double> D, Dinv, grad;

@@ -223,6 +223,10 @@ DEV void psd_project(double (&S)[N][N]) {
     }
 }
 
+// The 9x9 projection of mollified edge-edge pairs, out of line: the rare path stays out of
+// the register allocation of the kernels that contain it.
+static __device__ __noinline__ void psd_project9(double (&S)[9][9]) { psd_project<9>(S); }
+
 // Eigen-projection of a small symmetric matrix held in registers (fully unrolled
 // cyclic Jacobi on the upper triangle; N <= 5). Returns whether any eigenvalue was
 // negative (then S holds the projection), leaving S untouched otherwise.
@@ -302,14 +306,28 @@ DEV bool psd_project_small(double (&S)[N][N]) {
   return true;
 }
 
+// Destinations of a reduced 9x9 Hessian S (symmetric; producers give the entries with
+// p <= q): a local array (both triangles written) or the upper triangle of a per-pair
+// record in global memory (structure of arrays, entry k of pair i at base[k * stride + i]).
+DEV int s9_index(int p, int q) { return p * 9 - (p * (p - 1)) / 2 + (q - p); }  // p <= q, 0..44
+DEV void s9_put(double (&S)[9][9], int p, int q, double v) {
+  S[p][q] = v;
+  S[q][p] = v;
+}
+struct S9Rec {
+  double* base;
+  size_t stride;
+};
+DEV void s9_put(const S9Rec& o, int p, int q, double v) { o.base[(size_t)s9_index(p, q) * o.stride] = v; }
+
 // Reduced projection of a non-mollified pair: H lives in the span of
 // { c (x) e_x, c (x) e_y, c (x) e_z, a_k' (x) w } (a_k' = the parameter directions
 // orthonormalised against c; at most 3 + m <= 5 columns), where
 //   S_r = [[2 b' |c|^2 I + 4 b'' |c|^2 w w^T, 0], [0, 0]] - b' Phi_r G^-1 Phi_r^T.
 // S_r is projected (analytically for m = 0) and written back in the 9-dim Q (x) I basis.
-template <int M>
+template <int M, class Out>
 DEV void reduced_project(const Stencil& st, d3 w, const d3* W, const double (&Gi)[2][2], double B1, double B2,
-                         bool psd, double (&S9)[9][9]) {
+                         bool psd, Out& S9) {
   constexpr int N = 3 + M;
   double cn2 = 0;
 #pragma unroll
@@ -406,45 +424,45 @@ DEV void reduced_project(const Stencil& st, d3 w, const d3* W, const double (&Gi
     }
   }
   // back to the 9-dim basis: column alpha of the reduced basis has Q-coordinates
-  // (Q^T u_alpha) (x) v_alpha
-  double Bq[9][N];
+  // (Q^T u_alpha) (x) v_alpha, i.e. (Q^T c_hat) (x) e_r for alpha = r < 3 and
+  // (Q^T a_hat_l) (x) w_hat for alpha = 3 + l. With cq = Q^T c_hat, aq_l = Q^T a_hat_l:
+  //   S9[3a+r][3b+s] = cq_a cq_b Sr[r][s] + cq_a w_s al[b][r] + cq_b w_r al[a][s]
+  //                    + w_r w_s be[a][b],
+  //   al[a][r] = sum_l aq_l[a] Sr[r][3+l],  be[a][b] = sum_{l,l'} aq_l[a] Sr[3+l][3+l'] aq_l'[b].
   double cq[3];
   qt4(ch, cq);
-  double whv[3] = {wh.x, wh.y, wh.z};
+  const double whv[3] = {wh.x, wh.y, wh.z};
+  double aq[2][3] = {{0, 0, 0}, {0, 0, 0}};
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+  for (int l = 0; l < M; ++l) qt4(ah[l], aq[l]);
+  double al[3][3], be[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
+      double acc = 0;
 #pragma unroll
-      for (int j = 0; j < 3; ++j) Bq[3 * a + r][j] = (r == j) ? cq[a] : 0.0;
+      for (int l = 0; l < M; ++l) acc += aq[l][a] * Sr[r][3 + l];
+      al[a][r] = acc;
     }
 #pragma unroll
-  for (int l = 0; l < M; ++l) {
-    double aq[3];
-    qt4(ah[l], aq);
+    for (int b = 0; b < 3; ++b) {
+      double acc = 0;
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+      for (int l = 0; l < M; ++l)
 #pragma unroll
-      for (int r = 0; r < 3; ++r) Bq[3 * a + r][3 + l] = aq[a] * whv[r];
+        for (int l2 = 0; l2 < M; ++l2) acc += aq[l][a] * Sr[3 + l][3 + l2] * aq[l2][b];
+      be[a][b] = acc;
+    }
   }
-  double T[9][N];
 #pragma unroll
   for (int p = 0; p < 9; ++p)
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      double acc = 0;
-#pragma unroll
-      for (int i = 0; i < N; ++i) acc += Bq[p][i] * Sr[i][j];
-      T[p][j] = acc;
-    }
-#pragma unroll
-  for (int p = 0; p < 9; ++p)
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      double acc = 0;
-#pragma unroll
-      for (int j = 0; j < N; ++j) acc += T[p][j] * Bq[q][j];
-      S9[p][q] = acc;
+    for (int q = p; q < 9; ++q) {
+      const int a = p / 3, r = p % 3, b = q / 3, s = q % 3;
+      double v = cq[a] * cq[b] * (r <= s ? Sr[r][s] : Sr[s][r]);
+      if (M > 0) v += cq[a] * whv[s] * al[b][r] + cq[b] * whv[r] * al[a][s] + whv[r] * whv[s] * be[a][b];
+      s9_put(S9, p, q, v);
     }
 }
 
@@ -578,8 +596,9 @@ DEV void friction_2x2(const double* uk2, double lam, const FrictionP& fp, double
 
 // Reduced 9x9 Hessian S of a pair. Returns the vertex-space gradient g[4] (3-vectors).
 // kind 0: point-triangle, 1: edge-edge (mollified when the edges are near parallel).
+template <class Out>
 DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& bp, double eps_x_param, bool psd,
-                      double (&S)[9][9], d3* g) {
+                      Out& S, d3* g) {
   Stencil st;
   if (kind == 0) st_pt(X, ty, st);
   else st_ee(X, ty, st);
@@ -665,6 +684,7 @@ DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& b
     for (int i = 0; i < 4; ++i) g[i] = fscl(B1 * 2 * st.c[i], w);
     return;
   }
+  double Sm[9][9];
   for (int p = 0; p < 9; ++p)
     for (int q = 0; q < 9; ++q) {
       int a = p / 3, r = p % 3, b = q / 3, s = q % 3;
@@ -672,13 +692,13 @@ DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& b
       for (int k = 0; k < st.m; ++k)
         for (int l = 0; l < st.m; ++l) hd -= Phi[k][p] * Gi[k][l] * Phi[l][q];
       double h = mol * (B2 * gd[p] * gd[q] + B1 * hd);
-      if (mollified) {
-        double gmp = m1 * gx[p], gmq = m1 * gx[q];
-        h += (m2 * gx[p] * gx[q] + m1 * Hx[p][q]) * B + B1 * (gmp * gd[q] + gd[p] * gmq);
-      }
-      S[p][q] = h;
+      double gmp = m1 * gx[p], gmq = m1 * gx[q];
+      h += (m2 * gx[p] * gx[q] + m1 * Hx[p][q]) * B + B1 * (gmp * gd[q] + gd[p] * gmq);
+      Sm[p][q] = h;
     }
-  if (psd) psd_project<9>(S);
+  if (psd) psd_project9(Sm);
+  for (int p = 0; p < 9; ++p)
+    for (int q = p; q < 9; ++q) s9_put(S, p, q, Sm[p][q]);
   // vertex-space gradient: mol b' grad d + b grad mol
 #pragma unroll
   for (int i = 0; i < 4; ++i) g[i] = fscl(mol * B1 * 2 * st.c[i], w);
@@ -690,24 +710,26 @@ DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& b
   }
 }
 
-// Adds friction to the reduced Hessian and to the vertex gradient.
-DEV void pair_friction(const FrictionFrame& fr, const double* uk, double lam, const FrictionP& fp, double (&S)[9][9],
-                       d3* g) {
+// Friction of a pair: adds its force to the vertex gradient and returns its reduced
+// Hessian in factored form, S9[3a+r][3b+s] += gh[a] gh[b] N[r][s] (gh = Q^T gamma,
+// N = P M P^T with the tangent basis P and the 2x2 friction Hessian M); N6 holds the
+// upper triangle of N row by row.
+DEV void pair_friction(const FrictionFrame& fr, const double* uk, double lam, const FrictionP& fp, d3* g,
+                       double (&gh)[3], double (&N6)[6]) {
   double gs, M[2][2];
   friction_2x2(uk, lam, fp, gs, M);
   d3 F = fadd(fscl(gs * uk[0], fr.c0), fscl(gs * uk[1], fr.c1));
 #pragma unroll
   for (int i = 0; i < 4; ++i) g[i] = fadd(g[i], fscl(fr.gam[i], F));
-  double N[3][3];
+  int k = 0;
+#pragma unroll
   for (int r = 0; r < 3; ++r)
-    for (int s = 0; s < 3; ++s) {
+#pragma unroll
+    for (int s = r; s < 3; ++s) {
       double p0r = c3(fr.c0, r), p1r = c3(fr.c1, r), p0s = c3(fr.c0, s), p1s = c3(fr.c1, s);
-      N[r][s] = p0r * (M[0][0] * p0s + M[0][1] * p1s) + p1r * (M[1][0] * p0s + M[1][1] * p1s);
+      N6[k++] = p0r * (M[0][0] * p0s + M[0][1] * p1s) + p1r * (M[1][0] * p0s + M[1][1] * p1s);
     }
-  double gh[3];
   qt4(fr.gam, gh);
-  for (int p = 0; p < 9; ++p)
-    for (int q = 0; q < 9; ++q) S[p][q] += gh[p / 3] * gh[q / 3] * N[p % 3][q % 3];
 }
 
 }  // namespace abd

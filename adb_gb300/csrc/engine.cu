@@ -146,6 +146,7 @@ struct Engine {
     nbufs.x.release(); nbufs.r.release(); nbufs.z.release(); nbufs.p.release(); nbufs.qv.release();
     nbufs.Hrow.release(); nbufs.rcol.release(); nbufs.rn.release();
     nbufs.perm.release(); nbufs.cls_cnt.release(); nbufs.cls_off.release(); nbufs.cls_tmp.release();
+    nbufs.prec.release();
     nbufs.gpA.release(); nbufs.gpB.release(); nbufs.grp_body.release(); nbufs.grp_n.release();
     nbufs.grp_scene.release(); nbufs.sc_gbeg.release(); nbufs.sc_gend.release(); nbufs.sc_rz.release(); nbufs.sc_bb.release();
     nbufs.sc_conv.release(); nbufs.sc_iters.release(); nbufs.n_active.release();

@@ -24,55 +24,59 @@ inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 // ---------------------------------------------------------------------------------
 // Per-pair terms. kind 0: PT (point on body A, triangle on body B); 1: EE.
-// Stencil class of a pair (parameters of its closest-point problem, m = 0, 1, 2): the
-// size of the projection `pair_reduced` runs. PT: vertex-vertex 0-2, vertex-edge 3-5,
-// face 6; EE: vertex-vertex 0-3, vertex-edge 4-7, edge-edge 8.
-__device__ __forceinline__ int stencil_class(int kind, int ty) {
-  return kind == 0 ? (ty <= 2 ? 0 : (ty <= 5 ? 1 : 2)) : (ty <= 3 ? 0 : (ty <= 7 ? 1 : 2));
-}
+// Pairs are processed grouped by distance type (PT: 0-6, EE: 0-8), so that a warp runs
+// one branch of the type-dependent code (stencil, friction frame) and one projection
+// size (the stencil's parameter count m = 0, 1, 2 follows from the type). Mollified
+// edge-edge pairs (near-parallel edges, the full 9x9 projection) form a class of their
+// own, so their long projections occupy a few warps instead of slowing many.
+constexpr int NCLS = 10;
 constexpr int CLS_T = 256;
 
-// Pairs per stencil class in each block of CLS_T pairs: cnt[c * nblk + block].
-__global__ void k_class_count(int kind, int n, const int8_t* ty, int* cnt) {
-  __shared__ int sc[3];
-  if (threadIdx.x < 3) sc[threadIdx.x] = 0;
+__device__ __forceinline__ int pair_class(const Geo& g, const Params& P, int kind, const int* tup, const int8_t* ty,
+                                          int p);
+
+// Pairs per class in each block of CLS_T pairs: cnt[class * nblk + block].
+__global__ void k_class_count(Geo g, Params P, int kind, int n, const int* tup, const int8_t* ty, int* cnt) {
+  __shared__ int sc[NCLS];
+  if (threadIdx.x < NCLS) sc[threadIdx.x] = 0;
   __syncthreads();
   int p = blockIdx.x * CLS_T + threadIdx.x;
-  if (p < n) atomicAdd(&sc[stencil_class(kind, ty[p])], 1);
+  if (p < n) atomicAdd(&sc[pair_class(g, P, kind, tup, ty, p)], 1);
   __syncthreads();
-  if (threadIdx.x < 3) cnt[threadIdx.x * gridDim.x + blockIdx.x] = sc[threadIdx.x];
+  if (threadIdx.x < NCLS) cnt[threadIdx.x * gridDim.x + blockIdx.x] = sc[threadIdx.x];
 }
 
-// Stable partition of the pairs by stencil class (offsets from the scan of k_class_count),
-// so that the warps of k_pair_terms run a single projection size.
-__global__ void k_class_scatter(int kind, int n, const int8_t* ty, const int* off, int* perm) {
-  __shared__ int wc[3][CLS_T / 32];
+// Stable partition of the pairs by class (offsets from the scan of k_class_count).
+__global__ void k_class_scatter(Geo g, Params P, int kind, int n, const int* tup, const int8_t* ty, const int* off,
+                                int* perm) {
+  __shared__ int wc[NCLS][CLS_T / 32];
   const int p = blockIdx.x * CLS_T + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int c = p < n ? stencil_class(kind, ty[p]) : -1;
-  unsigned m[3];
+  const int c = p < n ? pair_class(g, P, kind, tup, ty, p) : -1;
+  unsigned mine = 0;
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    m[k] = __ballot_sync(0xffffffffu, c == k);
-    if (lane == 0) wc[k][w] = __popc(m[k]);
+  for (int k = 0; k < NCLS; ++k) {
+    unsigned m = __ballot_sync(0xffffffffu, c == k);
+    if (c == k) mine = m;
+    if (lane == 0) wc[k][w] = __popc(m);
   }
   __syncthreads();
   if (c >= 0) {
-    int r = off[c * gridDim.x + blockIdx.x] + __popc(m[c] & ((1u << lane) - 1u));
+    int r = off[c * gridDim.x + blockIdx.x] + __popc(mine & ((1u << lane) - 1u));
     for (int i = 0; i < w; ++i) r += wc[c][i];
     perm[r] = p;
   }
 }
 
-__global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, int n, const int* tup,
-                                                    const int* pov, const int* ovI, double* C, double* lag,
-                                                    const int* perm) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int p = perm[t];
-  int A = tup[4 * p], a = tup[4 * p + 1], B = tup[4 * p + 2], b = tup[4 * p + 3];
-  if (!scene_on(g, A)) return;  // scene not iterating: its blocks are not used
-  int vid[4];
-  int na;
+// Per-pair record between the two pair-term kernels (structure of arrays, stride = pairs):
+// the reduced Hessian's upper triangle (45), the vertex gradient (12), the friction
+// factors gh (3) and N (6, upper triangle) and an activity flag (1).
+enum { REC_S = 0, REC_G = 45, REC_GH = 57, REC_N = 60, REC_ACT = 66, REC = 67 };
+
+__device__ __forceinline__ void pair_vertices(const Geo& g, int kind, const int* tup, int p, int (&vid)[4], int& na,
+                                              int& A, int& B) {
+  A = tup[4 * p];
+  B = tup[4 * p + 2];
+  const int a = tup[4 * p + 1], b = tup[4 * p + 3];
   if (kind == 0) {
     vid[0] = g.v_off[A] + a;
     int f = g.f_off[B] + b;
@@ -88,16 +92,44 @@ __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, i
     vid[3] = g.ev[2 * eb + 1];
     na = 2;
   }
+}
+
+// Class of a pair for the grouping above: 0 for an edge-edge pair inside the
+// mollifier's range (the test of pair_reduced; first, so that their long projections
+// start with the first CTAs and overlap the rest), else 1 + its distance type.
+__device__ __forceinline__ int pair_class(const Geo& g, const Params& P, int kind, const int* tup, const int8_t* ty,
+                                          int p) {
+  int t = ty[p];
+  t = 1 + (t < 0 ? 0 : (t > NCLS - 2 ? NCLS - 2 : t));
+  if (kind == 1) {
+    int vid[4], na, A, B;
+    pair_vertices(g, kind, tup, p, vid, na, A, B);
+    d3 x0 = ldX(g.X, g.nv, vid[0]), x1 = ldX(g.X, g.nv, vid[1]);
+    d3 x2 = ldX(g.X, g.nv, vid[2]), x3 = ldX(g.X, g.nv, vid[3]);
+    d3 u = fsub(x1, x0), v = fsub(x3, x2);
+    double eps_x = P.eps_x * fdot(u, u) * fdot(v, v);
+    d3 cr = fcross(u, v);
+    if (fdot(cr, cr) < eps_x) t = 0;
+  }
+  return t;
+}
+
+// Per-pair terms, part 1 (kind 0: PT, point on body A, triangle on body B; 1: EE): the
+// barrier's reduced Hessian and gradient, the lagged friction frame and the friction
+// terms, written to the pair's record. Threads take pairs in stencil-class order (perm).
+__global__ void __launch_bounds__(128) k_pair_hess(Geo g, Params P, int kind, int n, const int* tup, const int* perm,
+                                                   double* R, double* lag) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int p = perm[t];
+  int vid[4], na, A, B;
+  pair_vertices(g, kind, tup, p, vid, na, A, B);
+  if (!scene_on(g, A)) return;  // scene not iterating: its blocks are not used
   d3 X[4], X0[4];
-  double xt[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     X[i] = ldX(g.X, g.nv, vid[i]);
     X0[i] = ldX(g.X0, g.nv, vid[i]);
-    xt[i][0] = 1.0;
-    xt[i][1] = g.rest[3 * vid[i]];
-    xt[i][2] = g.rest[3 * vid[i] + 1];
-    xt[i][3] = g.rest[3 * vid[i] + 2];
   }
   int ty;
   double d;
@@ -108,11 +140,11 @@ __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, i
     ty = ee_type(X[0], X[1], X[2], X[3]);
     d = ee_dist(X[0], X[1], X[2], X[3], ty);
   }
-  double S[9][9];
+  const size_t N = n;
   d3 gv[4];
   FrictionFrame fr;
   double lam = 0.0;
-  bool active = d < P.dhat;
+  const bool active = d < P.dhat;
   if (active) {
     BarrierP bp{P.dhat, P.kappa};
     if (kind == 0) frame_pt(X, ty, fr);
@@ -125,48 +157,83 @@ __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, i
       uk[1] += fr.gam[i] * fdot(fr.c1, du);
     }
     lam = -barrier_b1(d, bp) * 2 * sqrt(d);
-    pair_reduced(kind, ty, X, d, bp, P.eps_x, P.psd != 0, S, gv);
+    S9Rec rec{R + REC_S * N + p, N};
+    pair_reduced(kind, ty, X, d, bp, P.eps_x, P.psd != 0, rec, gv);
     if (!(P.terms & TERM_BARRIER)) {
-      for (int i = 0; i < 9; ++i)
-        for (int j = 0; j < 9; ++j) S[i][j] = 0.0;
+      for (int k = 0; k < 45; ++k) R[(REC_S + k) * N + p] = 0.0;
       for (int i = 0; i < 4; ++i) gv[i] = fd3(0, 0, 0);
     }
+    double gh[3] = {0, 0, 0}, N6[6] = {0, 0, 0, 0, 0, 0};
     bool fric = ((kind == 0) ? P.pt_fric : P.ee_fric) && (P.terms & TERM_FRICTION);
-    if (fric) pair_friction(fr, uk, lam, FrictionP{P.mu, P.epsv, P.max_uk}, S, gv);
+    if (fric) pair_friction(fr, uk, lam, FrictionP{P.mu, P.epsv, P.max_uk}, gv, gh, N6);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      R[(REC_G + 3 * i) * N + p] = gv[i].x;
+      R[(REC_G + 3 * i + 1) * N + p] = gv[i].y;
+      R[(REC_G + 3 * i + 2) * N + p] = gv[i].z;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) R[(REC_GH + k) * N + p] = gh[k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) R[(REC_N + k) * N + p] = N6[k];
   } else {
     fr.c0 = fd3(0, 0, 0);
     fr.c1 = fd3(0, 0, 0);
     for (int i = 0; i < 4; ++i) fr.gam[i] = 0;
   }
+  R[REC_ACT * N + p] = active ? 1.0 : 0.0;
   // lagged friction record
-  lag[0 * n + p] = fr.c0.x; lag[1 * n + p] = fr.c0.y; lag[2 * n + p] = fr.c0.z;
-  lag[3 * n + p] = fr.c1.x; lag[4 * n + p] = fr.c1.y; lag[5 * n + p] = fr.c1.z;
-  for (int i = 0; i < 4; ++i) lag[(6 + i) * n + p] = fr.gam[i];
-  lag[10 * n + p] = lam;
+  lag[0 * N + p] = fr.c0.x; lag[1 * N + p] = fr.c0.y; lag[2 * N + p] = fr.c0.z;
+  lag[3 * N + p] = fr.c1.x; lag[4 * N + p] = fr.c1.y; lag[5 * N + p] = fr.c1.z;
+  for (int i = 0; i < 4; ++i) lag[(6 + i) * N + p] = fr.gam[i];
+  lag[10 * N + p] = lam;
+}
 
-  int I = ovI[pov[p]];
-  bool a_is_I = (A == I);
-  bool a_dyn = g.mass[A] > 0.0, b_dyn = g.mass[B] > 0.0;
+// Per-pair terms, part 2: the chain rule onto the 12 affine DOFs of the two bodies,
+// d_A = Y_A S Y_A^T, d_B = Y_B S Y_B^T, off = Y_A S Y_B^T with Y_b[k][a] = sum over the
+// pair's vertices i on body b of xbar~_i[k] Q[i][a], and the body gradients.
+// S is symmetric, so for r < s one 3x3 slice M = S[3a+r][3b+s] gives the (r, s) and
+// (s, r) entries of all three blocks (d_A, d_B mirrored; off via M^T), and for r = s
+// only k <= l is formed for d_A and d_B.
+__global__ void __launch_bounds__(128) k_pair_chain(Geo g, int kind, int n, const int* tup, const int* pov,
+                                                    const int* ovI, const double* R, double* C) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  int vid[4], na, A, B;
+  pair_vertices(g, kind, tup, p, vid, na, A, B);
+  if (!scene_on(g, A)) return;
+  const size_t N = n;
+  const int I = ovI[pov[p]];
+  const bool a_is_I = (A == I);
+  const bool a_dyn = g.mass[A] > 0.0, b_dyn = g.mass[B] > 0.0;
   double* dI = C;
-  double* dJ = C + 144 * (size_t)n;
-  double* off = C + 288 * (size_t)n;
-  double* gI = C + 432 * (size_t)n;
-  double* gJ = C + 444 * (size_t)n;
+  double* dJ = C + 144 * N;
+  double* off = C + 288 * N;
+  double* gI = C + 432 * N;
+  double* gJ = C + 444 * N;
   double* dA = a_is_I ? dI : dJ;
   double* dB = a_is_I ? dJ : dI;
   double* gA = a_is_I ? gI : gJ;
   double* gB = a_is_I ? gJ : gI;
-  if (!active) {
+  if (R[REC_ACT * N + p] == 0.0) {
     for (int e = 0; e < 144; ++e) {
-      dI[(size_t)e * n + p] = 0.0;
-      dJ[(size_t)e * n + p] = 0.0;
-      off[(size_t)e * n + p] = 0.0;
+      dI[e * N + p] = 0.0;
+      dJ[e * N + p] = 0.0;
+      off[e * N + p] = 0.0;
     }
     for (int e = 0; e < 12; ++e) {
-      gI[(size_t)e * n + p] = 0.0;
-      gJ[(size_t)e * n + p] = 0.0;
+      gI[e * N + p] = 0.0;
+      gJ[e * N + p] = 0.0;
     }
     return;
+  }
+  double xt[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    xt[i][0] = 1.0;
+    xt[i][1] = g.rest[3 * vid[i]];
+    xt[i][2] = g.rest[3 * vid[i] + 1];
+    xt[i][3] = g.rest[3 * vid[i] + 2];
   }
   // Y matrices of the chain rule
   double YA[4][3], YB[4][3];
@@ -184,13 +251,26 @@ __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, i
       YA[k][aa] = sa;
       YB[k][aa] = sb;
     }
-  for (int r = 0; r < 3; ++r)
-    for (int s = 0; s < 3; ++s) {
+  double gh[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) gh[k] = R[(REC_GH + k) * N + p];
+  const bool off_on = a_dyn && b_dyn;
+  // one (r, s) slice at a time keeps the live state to Y, T and M
+#pragma unroll 1
+  for (int nidx = 0; nidx < 6; ++nidx) {
+    const int r = nidx < 3 ? 0 : (nidx < 5 ? 1 : 2);
+    const int s = nidx < 3 ? nidx : (nidx < 5 ? nidx - 2 : 2);
+    {
+      const double Nrs = R[(REC_N + nidx) * N + p];
       double M[3][3];
 #pragma unroll
       for (int aa = 0; aa < 3; ++aa)
 #pragma unroll
-        for (int bb = 0; bb < 3; ++bb) M[aa][bb] = S[3 * aa + r][3 * bb + s];
+        for (int bb = 0; bb < 3; ++bb) {
+          const int pp = 3 * aa + r, qq = 3 * bb + s;
+          const int e = pp <= qq ? s9_index(pp, qq) : s9_index(qq, pp);
+          M[aa][bb] = R[(REC_S + e) * N + p] + gh[aa] * gh[bb] * Nrs;
+        }
       double TA[4][3], TB[4][3];
 #pragma unroll
       for (int k = 0; k < 4; ++k)
@@ -203,17 +283,31 @@ __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, i
       for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
-          double aa_ = TA[k][0] * YA[l][0] + TA[k][1] * YA[l][1] + TA[k][2] * YA[l][2];
-          double bb_ = TB[k][0] * YB[l][0] + TB[k][1] * YB[l][1] + TB[k][2] * YB[l][2];
+          const int e = (3 * k + r) * 12 + (3 * l + s);
+          const int et = (3 * l + s) * 12 + (3 * k + r);
+          if (r < s || k <= l) {
+            double aa_ = TA[k][0] * YA[l][0] + TA[k][1] * YA[l][1] + TA[k][2] * YA[l][2];
+            double bb_ = TB[k][0] * YB[l][0] + TB[k][1] * YB[l][1] + TB[k][2] * YB[l][2];
+            dA[e * N + p] = a_dyn ? aa_ : 0.0;
+            dB[e * N + p] = b_dyn ? bb_ : 0.0;
+            if (e != et) {
+              dA[et * N + p] = a_dyn ? aa_ : 0.0;
+              dB[et * N + p] = b_dyn ? bb_ : 0.0;
+            }
+          }
+          // (A row (k, r), B column (l, s)), stored as block (I, J)
           double ab_ = TA[k][0] * YB[l][0] + TA[k][1] * YB[l][1] + TA[k][2] * YB[l][2];
-          int e = (3 * k + r) * 12 + (3 * l + s);
-          int et = (3 * l + s) * 12 + (3 * k + r);
-          dA[(size_t)e * n + p] = a_dyn ? aa_ : 0.0;
-          dB[(size_t)e * n + p] = b_dyn ? bb_ : 0.0;
-          // block (A, B) -> stored as block (I, J)
-          off[(size_t)(a_is_I ? e : et) * n + p] = (a_dyn && b_dyn) ? ab_ : 0.0;
+          off[(a_is_I ? e : et) * N + p] = off_on ? ab_ : 0.0;
+          if (r < s) {
+            // (A row (k, s), B column (l, r)) = Y_A[k] M^T Y_B[l]^T
+            const int e2 = (3 * k + s) * 12 + (3 * l + r);
+            const int et2 = (3 * l + r) * 12 + (3 * k + s);
+            double ba_ = TB[l][0] * YA[k][0] + TB[l][1] * YA[k][1] + TB[l][2] * YA[k][2];
+            off[(a_is_I ? e2 : et2) * N + p] = off_on ? ba_ : 0.0;
+          }
         }
     }
+  }
   // body gradients
 #pragma unroll
   for (int k = 0; k < 4; ++k)
@@ -222,12 +316,12 @@ __global__ void __launch_bounds__(128) k_pair_terms(Geo g, Params P, int kind, i
       double sa = 0, sb = 0;
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        double v = xt[i][k] * c3(gv[i], r);
+        double v = xt[i][k] * R[(REC_G + 3 * i + r) * N + p];
         if (i < na) sa += v;
         else sb += v;
       }
-      gA[(size_t)(3 * k + r) * n + p] = a_dyn ? sa : 0.0;
-      gB[(size_t)(3 * k + r) * n + p] = b_dyn ? sb : 0.0;
+      gA[(3 * k + r) * N + p] = a_dyn ? sa : 0.0;
+      gB[(3 * k + r) * N + p] = b_dyn ? sb : 0.0;
     }
 }
 
@@ -557,38 +651,16 @@ __global__ void k_pcg_rows(int nb, const int* row_ptr, const int* col, const int
   }
 }
 
-// CTA-wide sums of v[2k], v[2k+1] over k in [beg, end) (thread t takes beg + t,
-// beg + t + NT, ..., then a shuffle tree and the warps in order); every thread gets them.
-__device__ __forceinline__ void cta_sum2(const double* v, int beg, int end, double& a, double& b, double* sh) {
-  double sa = 0.0, sb = 0.0;
-  for (int k = beg + (int)threadIdx.x; k < end; k += blockDim.x) {
-    sa += v[2 * k];
-    sb += v[2 * k + 1];
-  }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+// Sum of v[2k + comp] over the groups k in [beg, end) of a scene, by one warp: lane l
+// adds k = beg + l, beg + l + 32, ... in order, then a butterfly over the lanes; every
+// lane gets the total. (GB300 runs FP64 at 2 FMA per clock per SM, so a CTA-wide tree
+// over all warps costs far more than one warp doing it.)
+__device__ __forceinline__ double warp_scene_sum(const double* v, int comp, int beg, int end) {
+  double s = 0.0;
+  for (int k = beg + (int)(threadIdx.x & 31); k < end; k += 32) s += v[2 * k + comp];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    sa += __shfl_xor_sync(0xffffffffu, sa, o);
-    sb += __shfl_xor_sync(0xffffffffu, sb, o);
-  }
-  if (lane == 0) {
-    sh[2 * w] = sa;
-    sh[2 * w + 1] = sb;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double ta = 0, tb = 0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-      ta += sh[2 * i];
-      tb += sh[2 * i + 1];
-    }
-    sh[64] = ta;
-    sh[65] = tb;
-  }
-  __syncthreads();
-  a = sh[64];
-  b = sh[65];
-  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
 }
 
 // Block-wide sums of a and b (shuffle tree, then the warps in order); thread 0 gets them.
@@ -622,23 +694,32 @@ __device__ __forceinline__ double body_sum16(double v) {
   return v;
 }
 
-// Group partials: the bodies' (c0, c1) in order, written by thread 0 to gp[2 g].
-__device__ __forceinline__ void group_sum2(double c0, double c1, bool lead, int lb, int nbody, double* s_bp,
-                                          double* gp, int g) {
-  if (lead) {
-    s_bp[2 * lb] = c0;
-    s_bp[2 * lb + 1] = c1;
+// Group partials from the per-row phase (threads 0 .. 16 GB - 1, two bodies per warp):
+// c0, c1 hold each body's sums on its 16 lanes; the warp adds its two bodies, thread 0
+// adds the warps in order and writes gp[2 g] (no write for g < 0). Ends with a CTA
+// barrier; called by every thread of the CTA.
+__device__ __forceinline__ void group_partial(double c0, double c1, double* s_w, double* gp, int g) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x < 16 * GB) {
+    c0 += __shfl_down_sync(0xffffffffu, c0, 16);
+    c1 += __shfl_down_sync(0xffffffffu, c1, 16);
+    if (lane == 0) {
+      s_w[2 * w] = c0;
+      s_w[2 * w + 1] = c1;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0 && g >= 0) {
-    double t0 = 0.0, t1 = 0.0;
-    for (int i = 0; i < nbody; ++i) {
-      t0 += s_bp[2 * i];
-      t1 += s_bp[2 * i + 1];
+    double t0 = s_w[0], t1 = s_w[1];
+#pragma unroll
+    for (int i = 1; i < GB / 2; ++i) {
+      t0 += s_w[2 * i];
+      t1 += s_w[2 * i + 1];
     }
     gp[2 * g] = t0;
     gp[2 * g + 1] = t1;
   }
+  __syncthreads();
 }
 
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
@@ -649,41 +730,45 @@ __device__ __forceinline__ double dir(double z, double beta, double p) { return 
 
 __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
   cg::grid_group grid = cg::this_grid();
-  __shared__ double sh[80];
   __shared__ double s_part[PCG_NT];
-  __shared__ double s_bp[2 * GB];
+  __shared__ double s_w[GB];                              // warp partials of group_partial
   __shared__ __align__(16) double s_v[PCG_NT / 16][12];  // direction entries of the block being read
+  __shared__ double s_sum[2];
   __shared__ double s_val;   // alpha or beta of this CTA's scene
   __shared__ int s_flag;     // 1: this CTA's scene does no work in this phase
   const int nloop = (a.ngrp + gridDim.x - 1) / gridDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int part = (threadIdx.x >> 4) & (NPART - 1), row = threadIdx.x & 15;
-  const int lb = threadIdx.x / BODY_SLOTS;   // body of the group
-  const int hg = threadIdx.x >> 4;           // 16-lane group of the CTA
-  const bool lead = part == 0 && row == 0;   // holds its body's partial sums
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // product phase: 64 threads per body (NPART groups of 16 lanes, lane = row)
+  const int part = (threadIdx.x >> 4) & (NPART - 1), prow = threadIdx.x & 15;
+  const int plb = threadIdx.x / BODY_SLOTS;
+  const int hg = threadIdx.x >> 4;
+  // per-row phases: threads 0 .. 16 GB - 1, body vlb = t / 16, row = t % 16
+  const bool vthr = threadIdx.x < 16 * GB;
+  const int vlb = threadIdx.x >> 4, row = threadIdx.x & 15;
 
-  // group handled in loop step `it`: g (or -1), its scene, this thread's body (or -1)
-  auto group = [&](int it, int& g, int& sc, int& body, int& nbody) {
+  // group handled in loop step `it`: g (or -1), its scene, first body, bodies
+  auto group = [&](int it, int& g, int& sc, int& b0, int& nbody) {
     g = blockIdx.x + it * gridDim.x;
     if (g >= a.ngrp) {
       g = -1;
       sc = -1;
-      body = -1;
+      b0 = 0;
       nbody = 0;
       return;
     }
     sc = a.grp_scene[g];
     nbody = a.grp_n[g];
-    body = lb < nbody ? a.grp_body[g] + lb : -1;
+    b0 = a.grp_body[g];
   };
 
   // ---- init: x = 0, r = b, z = M^-1 b, p_{-1} = 0 (zero for scenes not solved) ----
   for (int it = 0; it < nloop; ++it) {
-    int g, sc, body, nbody;
-    group(it, g, sc, body, nbody);
+    int g, sc, b0, nbody;
+    group(it, g, sc, b0, nbody);
     double c0 = 0.0, c1 = 0.0;
-    if (body >= 0 && part == 0 && row < 12) {
-      int idx = 12 * body + row;
+    if (vthr && g >= 0 && vlb < nbody && row < 12) {
+      const int body = b0 + vlb, idx = 12 * body + row;
       bool on = a.sc_on[sc] != 0;
       double bv = on ? a.b[idx] : 0.0;
       double zv = 0.0;
@@ -700,10 +785,11 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
       c0 = bv * bv;
       c1 = bv * zv;
     }
-    c0 = body_sum16(c0);
-    c1 = body_sum16(c1);
-    group_sum2(c0, c1, lead && body >= 0, lb, nbody, s_bp, a.gpB, g);
-    __syncthreads();
+    if (vthr) {
+      c0 = body_sum16(c0);
+      c1 = body_sum16(c1);
+    }
+    group_partial(c0, c1, s_w, a.gpB, g);
   }
   if (tid == 0) {
     a.n_active[0] = 0;
@@ -723,27 +809,40 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
     if (tid == 0) a.n_active[(k + 1) % 3] = 0;
     // ---- A_k: stopping test, beta, q = H p_k, p.q ----
     for (int it = 0; it < nloop; ++it) {
-      int g, sc, body, nbody;
-      group(it, g, sc, body, nbody);
+      int g, sc, b0, nbody;
+      group(it, g, sc, b0, nbody);
       if (g >= 0) {
-        const bool owner = g == a.sc_gbeg[sc];
-        if (k > 0 && conv_prev[sc]) {
-          if (threadIdx.x == 0) {
+        // scalars of the scene (thread 0 loads them while warps 0 and 1 reduce r.r, r.z)
+        int was_conv = 0, on = 1;
+        double bb = 0.0, rzp = 1.0;
+        if (threadIdx.x == 0) {
+          was_conv = k > 0 ? conv_prev[sc] : 0;
+          on = a.sc_on[sc];
+          if (k > 0) {
+            bb = a.sc_bb[sc];
+            rzp = rz_prev[sc];
+          }
+        }
+        if (warp < 2) {
+          double v = warp_scene_sum(a.gpB, warp, a.sc_gbeg[sc], a.sc_gend[sc]);
+          if (lane == 0) s_sum[warp] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          const bool owner = g == a.sc_gbeg[sc];
+          const double rr = s_sum[0], rz = s_sum[1];
+          if (was_conv) {
             if (owner) conv_cur[sc] = 1;
             s_flag = 1;
-          }
-        } else {
-          double rr, rz;
-          cta_sum2(a.gpB, a.sc_gbeg[sc], a.sc_gend[sc], rr, rz, sh);
-          if (threadIdx.x == 0) {
+          } else {
             bool conv;
             if (k == 0) {
-              conv = !a.sc_on[sc] || rr == 0.0;
+              conv = !on || rr == 0.0;
               if (owner) a.sc_bb[sc] = rr;
             } else {
-              conv = !(rr > a.tol2 * a.sc_bb[sc]);
+              conv = !(rr > a.tol2 * bb);
             }
-            s_val = k == 0 ? 0.0 : rz / rz_prev[sc];
+            s_val = k == 0 ? 0.0 : rz / rzp;
             s_flag = conv || k == a.maxit;
             if (owner) {
               rz_cur[sc] = rz;
@@ -764,17 +863,18 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
       const bool act = g >= 0 && !s_flag;
       const double beta = act ? s_val : 0.0;
       double acc = 0.0;
-      if (act && body >= 0) {
+      if (act && plb < nbody) {
         // the two 16-lane halves of a warp are different parts and may run different
         // trip counts: each half synchronises only itself
         const unsigned half = 0xffffu << (threadIdx.x & 16);
+        const int body = b0 + plb;
         const int base = body + a.row_ptr[body], n = a.rn[body];
         for (int j = part; j < n; j += NPART) {
           const int cb = a.rcol[base + j];
-          if (row < 12) s_v[hg][row] = dir(a.z[12 * cb + row], beta, p_old[12 * cb + row]);
+          if (prow < 12) s_v[hg][prow] = dir(a.z[12 * cb + prow], beta, p_old[12 * cb + prow]);
           __syncwarp(half);
-          if (row < 12) {
-            const double2* H = reinterpret_cast<const double2*>(a.Hrow + (size_t)(base + j) * 144 + 12 * row);
+          if (prow < 12) {
+            const double2* H = reinterpret_cast<const double2*>(a.Hrow + (size_t)(base + j) * 144 + 12 * prow);
             const double2* v = reinterpret_cast<const double2*>(s_v[hg]);
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
@@ -788,20 +888,22 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
       }
       s_part[threadIdx.x] = acc;
       __syncthreads();
-      double c0 = 0.0;
-      if (act && body >= 0 && part == 0 && row < 12) {
-        const double* sp = s_part + lb * BODY_SLOTS + row;
-        double qv = sp[0];
+      if (act) {
+        double c0 = 0.0;
+        if (vthr && vlb < nbody && row < 12) {
+          const double* sp = s_part + vlb * BODY_SLOTS + row;
+          double qv = sp[0];
 #pragma unroll
-        for (int pp = 1; pp < NPART; ++pp) qv += sp[16 * pp];
-        int idx = 12 * body + row;
-        double pv = dir(a.z[idx], beta, p_old[idx]);
-        p_new[idx] = pv;
-        a.q[idx] = qv;
-        c0 = pv * qv;
+          for (int pp = 1; pp < NPART; ++pp) qv += sp[16 * pp];
+          const int idx = 12 * (b0 + vlb) + row;
+          double pv = dir(a.z[idx], beta, p_old[idx]);
+          p_new[idx] = pv;
+          a.q[idx] = qv;
+          c0 = pv * qv;
+        }
+        if (vthr) c0 = body_sum16(c0);
+        group_partial(c0, 0.0, s_w, a.gpA, g);
       }
-      c0 = body_sum16(c0);
-      if (act) group_sum2(c0, 0.0, lead && body >= 0, lb, nbody, s_bp, a.gpA, g);
       __syncthreads();
     }
     if (k == a.maxit) break;
@@ -809,46 +911,53 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
     if (ld_volatile(&a.n_active[k % 3]) == 0) break;
     // ---- B_k: alpha; x += alpha p, r -= alpha q, z = M^-1 r; r.r, r.z ----
     for (int it = 0; it < nloop; ++it) {
-      int g, sc, body, nbody;
-      group(it, g, sc, body, nbody);
+      int g, sc, b0, nbody;
+      group(it, g, sc, b0, nbody);
       const bool act = g >= 0 && !conv_cur[sc];
-      if (act) {
-        double pq, dummy;
-        cta_sum2(a.gpA, a.sc_gbeg[sc], a.sc_gend[sc], pq, dummy, sh);
-        if (threadIdx.x == 0) s_val = rz_cur[sc] / pq;
+      if (act && warp == 0) {
+        const double rz = lane == 0 ? rz_cur[sc] : 0.0;
+        const double pq = warp_scene_sum(a.gpA, 0, a.sc_gbeg[sc], a.sc_gend[sc]);
+        if (lane == 0) s_val = rz / pq;
       }
       __syncthreads();
-      const bool mine = act && body >= 0 && part == 0 && row < 12;
-      const int idx = 12 * body + row;
-      if (mine) {
-        double alpha = s_val;
-        a.x[idx] += alpha * p_new[idx];
-        a.r[idx] -= alpha * a.q[idx];
-      }
-      __syncwarp();
-      double c0 = 0.0, c1 = 0.0;
-      if (mine) {
-        const double* Mi = a.Dinv + 144 * body + 12 * row;
-        double zv = 0;
+      if (act) {
+        double c0 = 0.0, c1 = 0.0;
+        const bool mine = vthr && vlb < nbody && row < 12;
+        const int body = b0 + vlb, idx = 12 * body + row;
+        if (mine) {
+          const double alpha = s_val;
+          a.x[idx] += alpha * p_new[idx];
+          a.r[idx] -= alpha * a.q[idx];
+        }
+        __syncwarp();
+        if (mine) {
+          const double* Mi = a.Dinv + 144 * body + 12 * row;
+          double zv = 0;
 #pragma unroll
-        for (int c = 0; c < 12; ++c) zv += Mi[c] * a.r[12 * body + c];
-        a.z[idx] = zv;
-        double rv = a.r[idx];
-        c0 = rv * rv;
-        c1 = rv * zv;
+          for (int c = 0; c < 12; ++c) zv += Mi[c] * a.r[12 * body + c];
+          a.z[idx] = zv;
+          double rv = a.r[idx];
+          c0 = rv * rv;
+          c1 = rv * zv;
+        }
+        if (vthr) {
+          c0 = body_sum16(c0);
+          c1 = body_sum16(c1);
+        }
+        group_partial(c0, c1, s_w, a.gpB, g);
       }
-      c0 = body_sum16(c0);
-      c1 = body_sum16(c1);
-      if (act) group_sum2(c0, c1, lead && body >= 0, lb, nbody, s_bp, a.gpB, g);
       __syncthreads();
     }
     grid.sync();
   }
   // dq = -x (each entry written by the thread that owns it)
   for (int it = 0; it < nloop; ++it) {
-    int g, sc, body, nbody;
-    group(it, g, sc, body, nbody);
-    if (body >= 0 && part == 0 && row < 12) a.dq[12 * body + row] = -a.x[12 * body + row];
+    int g, sc, b0, nbody;
+    group(it, g, sc, b0, nbody);
+    if (vthr && g >= 0 && vlb < nbody && row < 12) {
+      const int idx = 12 * (b0 + vlb) + row;
+      a.dq[idx] = -a.x[idx];
+    }
   }
   if (tid == 0) a.out[1] = k;
 }
@@ -1225,17 +1334,20 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
     int n = kind ? nee : npt;
     if (!n) continue;
     int nb_c = nblk(n, CLS_T);
-    B.cls_cnt.ensure(3 * (size_t)nb_c);
-    B.cls_off.ensure(3 * (size_t)nb_c);
+    B.cls_cnt.ensure(NCLS * (size_t)nb_c);
+    B.cls_off.ensure(NCLS * (size_t)nb_c);
     B.perm.ensure(n);
     const int8_t* ty = kind ? S.ee_ty.p : S.pt_ty.p;
-    KLAUNCH(K_SEG, s, k_class_count<<<nb_c, CLS_T, 0, s>>>(kind, n, ty, B.cls_cnt.p));
-    scan_exclusive_int(B.cls_cnt.p, B.cls_off.p, 3 * nb_c, nullptr, s, B.cls_tmp);
-    KLAUNCH(K_SEG, s, k_class_scatter<<<nb_c, CLS_T, 0, s>>>(kind, n, ty, B.cls_off.p, B.perm.p));
-    KLAUNCH(K_PAIR_TERMS, s, k_pair_terms<<<nblk(n, 128), 128, 0, s>>>(g, P, kind, n, kind ? S.ee.p : S.pt.p,
-                                                                     kind ? S.ee_ov.p : S.pt_ov.p, S.ovI.p,
-                                                                     kind ? B.ee_c.p : B.pt_c.p,
-                                                                     kind ? S.ee_lag.p : S.pt_lag.p, B.perm.p));
+    const int* tup = kind ? S.ee.p : S.pt.p;
+    KLAUNCH(K_SEG, s, k_class_count<<<nb_c, CLS_T, 0, s>>>(g, P, kind, n, tup, ty, B.cls_cnt.p));
+    scan_exclusive_int(B.cls_cnt.p, B.cls_off.p, NCLS * nb_c, nullptr, s, B.cls_tmp);
+    KLAUNCH(K_SEG, s, k_class_scatter<<<nb_c, CLS_T, 0, s>>>(g, P, kind, n, tup, ty, B.cls_off.p, B.perm.p));
+    B.prec.ensure(REC * (size_t)n);
+    KLAUNCH(K_PAIR_TERMS, s, k_pair_hess<<<nblk(n, 128), 128, 0, s>>>(g, P, kind, n, tup, B.perm.p, B.prec.p,
+                                                                    kind ? S.ee_lag.p : S.pt_lag.p));
+    KLAUNCH(K_PAIR_TERMS, s, k_pair_chain<<<nblk(n, 128), 128, 0, s>>>(g, kind, n, tup, kind ? S.ee_ov.p : S.pt_ov.p,
+                                                                     S.ovI.p, B.prec.p,
+                                                                     kind ? B.ee_c.p : B.pt_c.p));
   }
   if (nov) {
     KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, npt, S.pt_ov.p, B.pt_seg.p));
