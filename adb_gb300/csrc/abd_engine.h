@@ -222,6 +222,8 @@ struct NewtonBufs {
   DBuf<int> pt_seg, ee_seg;  // nov + 1
   DBuf<int> perm, cls_cnt, cls_off, cls_tmp;  // pairs in distance-type order
   DBuf<double> prec;         // per-pair reduced Hessian records between the pair-term kernels
+  cudaStream_t side = nullptr;               // mollified pairs run beside the main pair kernel
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   DBuf<double> ovr;          // nov * CONTRIB
   DBuf<int> has;             // nov
   DBuf<double> D, Dinv, grad;

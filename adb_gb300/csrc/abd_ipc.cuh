@@ -594,22 +594,61 @@ DEV void friction_2x2(const double* uk2, double lam, const FrictionP& fp, double
   }
 }
 
-// Reduced 9x9 Hessian S of a pair. Returns the vertex-space gradient g[4] (3-vectors).
-// kind 0: point-triangle, 1: edge-edge (mollified when the edges are near parallel).
-template <class Out>
-DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& bp, double eps_x_param, bool psd,
-                      Out& S, d3* g) {
-  Stencil st;
+// Everything a mollified edge-edge pair's 9x9 reduced Hessian is built from: the
+// distance's first and second derivatives (gd, Phi, Gi, ch), the barrier derivatives,
+// the mollifier m(x) with its derivatives and x's gradient gx, and the two edge vectors
+// (x's Hessian follows from them).
+struct MollData {
+  double gd[9], gx[9], Phi[2][9];
+  double ch[3], Gi[2][2];
+  double mol, B, B1, B2, m1, m2;
+  double u[3], v[3], uu, vv, uv;
+  int m;
+};
+
+// Entry (p, q) of x = |u x v|^2's Hessian in the reduced coordinates (u = 2 x_0..2,
+// v = x_3..5 directions, zero for 6..8).
+DEV double moll_hx(const MollData& md, int p, int q) {
+  if (p >= 6 || q >= 6) return 0.0;
+  const int i = p % 3, j = q % 3;
+  const double dij = (i == j) ? 1.0 : 0.0;
+  if (p < 3 && q < 3) return 2.0 * (2.0 * (md.vv * dij - md.v[i] * md.v[j]));
+  if (p >= 3 && q >= 3) return 2.0 * (2.0 * (md.uu * dij - md.u[i] * md.u[j]));
+  if (p < 3) return 2.0 * (2.0 * (2.0 * md.u[i] * md.v[j] - md.v[i] * md.u[j] - md.uv * dij));
+  return 2.0 * (2.0 * (2.0 * md.u[j] * md.v[i] - md.v[j] * md.u[i] - md.uv * dij));
+}
+
+// Entry (p, q) of a mollified pair's reduced Hessian (before projection):
+// m (b'' grad d grad d^T + b' hess d) + b (m'' grad x grad x^T + m' hess x)
+// + b' m' (grad x grad d^T + grad d grad x^T).
+DEV double moll_entry(const MollData& md, int p, int q) {
+  const int a = p / 3, r = p % 3, b = q / 3, s = q % 3;
+  double hd = (r == s ? 2 * md.ch[a] * md.ch[b] : 0.0);
+  for (int k = 0; k < md.m; ++k)
+    for (int l = 0; l < md.m; ++l) hd -= md.Phi[k][p] * md.Gi[k][l] * md.Phi[l][q];
+  double h = md.mol * (md.B2 * md.gd[p] * md.gd[q] + md.B1 * hd);
+  double gmp = md.m1 * md.gx[p], gmq = md.m1 * md.gx[q];
+  h += (md.m2 * md.gx[p] * md.gx[q] + md.m1 * moll_hx(md, p, q)) * md.B + md.B1 * (gmp * md.gd[q] + md.gd[p] * gmq);
+  return h;
+}
+
+// Shared set-up of pair_reduced: stencil, closest-point derivatives and, for edge-edge
+// pairs inside the mollifier's range, the mollifier data. Returns whether the pair is
+// mollified; for the others the outputs needed by reduced_project are set.
+DEV bool pair_setup(int kind, int ty, const d3* X, double d, const BarrierP& bp, double eps_x_param, Stencil& st,
+                    d3& w, d3 (&W)[2], double (&Gi)[2][2], MollData& md, d3& gu, d3& gv) {
   if (kind == 0) st_pt(X, ty, st);
   else st_ee(X, ty, st);
-  d3 w = fd3(0, 0, 0), W[2] = {fd3(0, 0, 0), fd3(0, 0, 0)};
+  w = fd3(0, 0, 0);
+  W[0] = fd3(0, 0, 0);
+  W[1] = fd3(0, 0, 0);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     w = fadd(w, fscl(st.c[i], X[i]));
     W[0] = fadd(W[0], fscl(st.a[0][i], X[i]));
     W[1] = fadd(W[1], fscl(st.a[1][i], X[i]));
   }
-  double Gi[2][2] = {{0, 0}, {0, 0}};
+  Gi[0][0] = Gi[0][1] = Gi[1][0] = Gi[1][1] = 0.0;
   if (st.m == 1) {
     Gi[0][0] = 1.0 / (2 * fdot(W[0], W[0]));
   } else if (st.m == 2) {
@@ -619,95 +658,93 @@ DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& b
     Gi[1][1] = g00 / det;
     Gi[0][1] = Gi[1][0] = -g01 / det;
   }
-  double ch[3], ah[2][3];
-  qt4(st.c, ch);
+  md.B1 = barrier_b1(d, bp);
+  md.B2 = barrier_b2(d, bp);
+  md.mol = 1.0;
+  md.B = md.m1 = md.m2 = 0.0;
+  gu = gv = fd3(0, 0, 0);
+  if (kind != 1) return false;
+  d3 u = fsub(X[1], X[0]), v = fsub(X[3], X[2]);
+  double eps_x = eps_x_param * fdot(fsub(X[0], X[1]), fsub(X[0], X[1])) * fdot(fsub(X[2], X[3]), fsub(X[2], X[3]));
+  d3 cr = fcross(u, v);
+  double x = fdot(cr, cr);
+  if (!(x < eps_x)) return false;
+  double xe = x / eps_x;
+  md.mol = (-xe + 2.0) * xe;
+  md.m1 = 2.0 * (1.0 - xe) / eps_x;
+  md.m2 = -2.0 / (eps_x * eps_x);
+  md.B = barrier_b(d, bp);
+  md.uu = fdot(u, u);
+  md.vv = fdot(v, v);
+  md.uv = fdot(u, v);
+  gu = fsub(fscl(2.0 * md.vv, u), fscl(2.0 * md.uv, v));
+  gv = fsub(fscl(2.0 * md.uu, v), fscl(2.0 * md.uv, u));
+  md.u[0] = u.x; md.u[1] = u.y; md.u[2] = u.z;
+  md.v[0] = v.x; md.v[1] = v.y; md.v[2] = v.z;
+  const double sq2 = 1.41421356237309504880;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    md.gx[r] = -sq2 * c3(gu, r);
+    md.gx[3 + r] = -sq2 * c3(gv, r);
+    md.gx[6 + r] = 0.0;
+  }
+  double ah[2][3];
+  qt4(st.c, md.ch);
   qt4(st.a[0], ah[0]);
   qt4(st.a[1], ah[1]);
-  double Phi[2][9];
-  double gd[9];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      gd[3 * a + r] = 2 * ch[a] * c3(w, r);
-      Phi[0][3 * a + r] = 2 * (ch[a] * c3(W[0], r) + ah[0][a] * c3(w, r));
-      Phi[1][3 * a + r] = 2 * (ch[a] * c3(W[1], r) + ah[1][a] * c3(w, r));
+      md.gd[3 * a + r] = 2 * md.ch[a] * c3(w, r);
+      md.Phi[0][3 * a + r] = 2 * (md.ch[a] * c3(W[0], r) + ah[0][a] * c3(w, r));
+      md.Phi[1][3 * a + r] = 2 * (md.ch[a] * c3(W[1], r) + ah[1][a] * c3(w, r));
     }
-  double B1 = barrier_b1(d, bp), B2 = barrier_b2(d, bp);
-  double mol = 1.0, B = 0.0, m1 = 0.0, m2 = 0.0;
-  double gx[9];
-  double Hx[9][9];
-  bool mollified = false;
-  d3 gu = fd3(0, 0, 0), gv = fd3(0, 0, 0);
-  if (kind == 1) {
-    d3 u = fsub(X[1], X[0]), v = fsub(X[3], X[2]);
-    double eps_x = eps_x_param * fdot(fsub(X[0], X[1]), fsub(X[0], X[1])) * fdot(fsub(X[2], X[3]), fsub(X[2], X[3]));
-    d3 cr = fcross(u, v);
-    double x = fdot(cr, cr);
-    if (x < eps_x) {
-      mollified = true;
-      double xe = x / eps_x;
-      mol = (-xe + 2.0) * xe;
-      m1 = 2.0 * (1.0 - xe) / eps_x;
-      m2 = -2.0 / (eps_x * eps_x);
-      B = barrier_b(d, bp);
-      double uu = fdot(u, u), vv = fdot(v, v), uv = fdot(u, v);
-      gu = fsub(fscl(2.0 * vv, u), fscl(2.0 * uv, v));
-      gv = fsub(fscl(2.0 * uu, v), fscl(2.0 * uv, u));
-      const double sq2 = 1.41421356237309504880;
-      for (int r = 0; r < 3; ++r) {
-        gx[r] = -sq2 * c3(gu, r);
-        gx[3 + r] = -sq2 * c3(gv, r);
-        gx[6 + r] = 0.0;
-      }
-      for (int i = 0; i < 9; ++i)
-        for (int j = 0; j < 9; ++j) Hx[i][j] = 0.0;
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-          double dij = (i == j) ? 1.0 : 0.0;
-          double huu = 2.0 * (vv * dij - c3(v, i) * c3(v, j));
-          double hvv = 2.0 * (uu * dij - c3(u, i) * c3(u, j));
-          double huv = 2.0 * (2.0 * c3(u, i) * c3(v, j) - c3(v, i) * c3(u, j) - uv * dij);
-          double hvu = 2.0 * (2.0 * c3(u, j) * c3(v, i) - c3(v, j) * c3(u, i) - uv * dij);
-          Hx[i][j] = 2.0 * huu;
-          Hx[3 + i][3 + j] = 2.0 * hvv;
-          Hx[i][3 + j] = 2.0 * huv;
-          Hx[3 + i][j] = 2.0 * hvu;
-        }
-    }
-  }
-  if (!mollified) {
-    if (st.m == 0) reduced_project<0>(st, w, W, Gi, B1, B2, psd, S);
-    else if (st.m == 1) reduced_project<1>(st, w, W, Gi, B1, B2, psd, S);
-    else reduced_project<2>(st, w, W, Gi, B1, B2, psd, S);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) g[i] = fscl(B1 * 2 * st.c[i], w);
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int l = 0; l < 2; ++l) md.Gi[k][l] = Gi[k][l];
+  md.m = st.m;
+  return true;
+}
+
+// Vertex-space gradient of a pair: m b' grad d + b grad m.
+DEV void pair_gradient(const Stencil& st, d3 w, const MollData& md, d3 gu, d3 gv, d3* g) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) g[i] = fscl(md.mol * md.B1 * 2 * st.c[i], w);
+  if (md.m1 != 0.0 || md.B != 0.0) {
+    g[0] = fsub(g[0], fscl(md.B * md.m1, gu));
+    g[1] = fadd(g[1], fscl(md.B * md.m1, gu));
+    g[2] = fsub(g[2], fscl(md.B * md.m1, gv));
+    g[3] = fadd(g[3], fscl(md.B * md.m1, gv));
+  }
+}
+
+// Reduced 9x9 Hessian S of a pair. Returns the vertex-space gradient g[4] (3-vectors).
+// kind 0: point-triangle, 1: edge-edge (mollified when the edges are near parallel).
+template <class Out>
+DEV void pair_reduced(int kind, int ty, const d3* X, double d, const BarrierP& bp, double eps_x_param, bool psd,
+                      Out& S, d3* g) {
+  Stencil st;
+  d3 w, W[2], gu, gv;
+  double Gi[2][2];
+  MollData md;
+  const bool mollified = pair_setup(kind, ty, X, d, bp, eps_x_param, st, w, W, Gi, md, gu, gv);
+  if (!mollified) {
+    if (st.m == 0) reduced_project<0>(st, w, W, Gi, md.B1, md.B2, psd, S);
+    else if (st.m == 1) reduced_project<1>(st, w, W, Gi, md.B1, md.B2, psd, S);
+    else reduced_project<2>(st, w, W, Gi, md.B1, md.B2, psd, S);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) g[i] = fscl(md.B1 * 2 * st.c[i], w);
     return;
   }
   double Sm[9][9];
   for (int p = 0; p < 9; ++p)
-    for (int q = 0; q < 9; ++q) {
-      int a = p / 3, r = p % 3, b = q / 3, s = q % 3;
-      double hd = (r == s ? 2 * ch[a] * ch[b] : 0.0);
-      for (int k = 0; k < st.m; ++k)
-        for (int l = 0; l < st.m; ++l) hd -= Phi[k][p] * Gi[k][l] * Phi[l][q];
-      double h = mol * (B2 * gd[p] * gd[q] + B1 * hd);
-      double gmp = m1 * gx[p], gmq = m1 * gx[q];
-      h += (m2 * gx[p] * gx[q] + m1 * Hx[p][q]) * B + B1 * (gmp * gd[q] + gd[p] * gmq);
-      Sm[p][q] = h;
-    }
+    for (int q = 0; q < 9; ++q) Sm[p][q] = moll_entry(md, p, q);
   if (psd) psd_project9(Sm);
   for (int p = 0; p < 9; ++p)
     for (int q = p; q < 9; ++q) s9_put(S, p, q, Sm[p][q]);
-  // vertex-space gradient: mol b' grad d + b grad mol
-#pragma unroll
-  for (int i = 0; i < 4; ++i) g[i] = fscl(mol * B1 * 2 * st.c[i], w);
-  if (mollified) {
-    g[0] = fsub(g[0], fscl(B * m1, gu));
-    g[1] = fadd(g[1], fscl(B * m1, gu));
-    g[2] = fsub(g[2], fscl(B * m1, gv));
-    g[3] = fadd(g[3], fscl(B * m1, gv));
-  }
+  pair_gradient(st, w, md, gu, gv, g);
 }
 
 // Friction of a pair: adds its force to the vertex gradient and returns its reduced

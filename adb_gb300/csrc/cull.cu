@@ -372,9 +372,8 @@ __device__ __forceinline__ SubLists sub_lists(const Geo& g, int sub, int I, int 
   return L;
 }
 
-// Block-wide union of float boxes (min of lo, max of hi); the result is broadcast.
-__device__ __forceinline__ void block_box_union(float* b, float* sh /* >= 6 * NT/32 + 6 */) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+// Warp-wide union of float boxes (min of lo, max of hi); every lane gets it.
+__device__ __forceinline__ void warp_box_union(float* b) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -382,30 +381,18 @@ __device__ __forceinline__ void block_box_union(float* b, float* sh /* >= 6 * NT
       float v = __shfl_xor_sync(0xffffffffu, b[c], o);
       b[c] = c < 3 ? fminf(b[c], v) : fmaxf(b[c], v);
     }
-  if (lane == 0)
-#pragma unroll
-    for (int c = 0; c < 6; ++c) sh[6 * w + c] = b[c];
-  __syncthreads();
-  if (threadIdx.x == 0)
-    for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
-#pragma unroll
-      for (int c = 0; c < 6; ++c) sh[c] = c < 3 ? fminf(sh[c], sh[6 * q + c]) : fmaxf(sh[c], sh[6 * q + c]);
-  __syncthreads();
-#pragma unroll
-  for (int c = 0; c < 6; ++c) b[c] = sh[c];
-  __syncthreads();
 }
 
 // Keeps, in order and in place, the entries of list L[0..n) whose float box (inflated by
-// ds when `infl`) hits box `q`; returns the new length. Writes never pass reads: each
-// chunk of NT entries is read before any of it is written.
-__device__ __forceinline__ int block_compact(int* L, int n, int off, const float* boxes, bool infl, float ds,
-                                             const float* q, int* sh /* >= NT/32 + 1 */) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+// ds when `infl`) hits box `q`; returns the new length. Each chunk of 32 entries is read
+// before any of it is written, and writes never pass reads.
+__device__ __forceinline__ int warp_compact(int* L, int n, int off, const float* boxes, bool infl, float ds,
+                                            const float* q) {
+  const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   int kept = 0;
-  for (int k0 = 0; k0 < n; k0 += NT) {
-    int k = k0 + threadIdx.x;
+  for (int k0 = 0; k0 < n; k0 += 32) {
+    int k = k0 + lane;
     int id = 0;
     bool keep = false;
     if (k < n) {
@@ -419,29 +406,29 @@ __device__ __forceinline__ int block_compact(int* L, int n, int off, const float
       keep = f_overlap(bx, q);
     }
     unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (lane == 0) sh[w] = __popc(m);
-    __syncthreads();
-    int pre = 0, tot = 0;
-#pragma unroll
-    for (int q2 = 0; q2 < NT / 32; ++q2) {
-      pre += q2 < w ? sh[q2] : 0;
-      tot += sh[q2];
-    }
-    if (keep) L[kept + pre + __popc(m & below)] = id;
-    kept += tot;
-    __syncthreads();
+    if (keep) L[kept + __popc(m & below)] = id;
+    kept += __popc(m);
   }
   return kept;
 }
 
-// Shrinks the two lists of a sub-problem so that every candidate pair whose float boxes
-// hit survives: A keeps the entries hitting the union of the B boxes, then B keeps the
-// entries hitting the union of the kept A boxes (A inflated by ds when `infl`). The
-// reference's loose body boxes bin whole caps of both bodies; this leaves the part near
-// the other body.
-__device__ void refine_lists(SubLists& L, int* nA_slot, int* nB_slot, bool infl, float ds, float* shf, int* shi) {
+// 4b. Shrinks the two lists of every sub-problem (one warp per overlap and sub-problem) so
+// that every candidate pair whose float boxes hit survives: A keeps the entries hitting
+// the union of the B boxes, then B keeps the entries hitting the union of the kept A boxes
+// (A inflated by ds for the pair cull, not for trajectories). The reference's loose body
+// boxes bin whole caps of both bodies; this leaves the part near the other body, and most
+// sub-problems of a pile end up empty before any CTA of the narrow phase is spent on them.
+template <bool INFL>
+__global__ void k_refine(Geo g, float ds, int nov, const int* ovI, const int* ovJ, int* cnt, const int* off, int* lst,
+                         const float* vb, const float* eb, const float* fb) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= 3 * nov) return;
+  const int u = warp / 3, sub = warp - 3 * u;
+  int* n = cnt + 6 * u;
+  SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, off + 6 * u, lst, vb, eb, fb);
+  if (L.nA == 0 || L.nB == 0) return;
   float bb[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-  for (int k = threadIdx.x; k < L.nB; k += NT) {
+  for (int k = lane; k < L.nB; k += 32) {
     const float* b = L.boxB + 6 * (L.offB + L.LB[k]);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -449,15 +436,15 @@ __device__ void refine_lists(SubLists& L, int* nA_slot, int* nB_slot, bool infl,
       bb[c + 3] = fmaxf(bb[c + 3], b[c + 3]);
     }
   }
-  block_box_union(bb, shf);
+  warp_box_union(bb);
   int* LA = const_cast<int*>(L.LA);
   int* LB = const_cast<int*>(L.LB);
-  L.nA = block_compact(LA, L.nA, L.offA, L.boxA, infl, ds, bb, shi);
+  const int nA = warp_compact(LA, L.nA, L.offA, L.boxA, INFL, ds, bb);
   float ba[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-  for (int k = threadIdx.x; k < L.nA; k += NT) {
+  for (int k = lane; k < nA; k += 32) {
     float a[6];
     const float* src = L.boxA + 6 * (L.offA + LA[k]);
-    if (infl) finflate(src, ds, a);
+    if (INFL) finflate(src, ds, a);
     else
 #pragma unroll
       for (int c = 0; c < 6; ++c) a[c] = src[c];
@@ -467,11 +454,12 @@ __device__ void refine_lists(SubLists& L, int* nA_slot, int* nB_slot, bool infl,
       ba[c + 3] = fmaxf(ba[c + 3], a[c + 3]);
     }
   }
-  block_box_union(ba, shf);
-  L.nB = L.nA ? block_compact(LB, L.nB, L.offB, L.boxB, false, ds, ba, shi) : 0;
-  if (threadIdx.x == 0) {
-    *nA_slot = L.nA;
-    *nB_slot = L.nB;
+  warp_box_union(ba);
+  const int nB = nA ? warp_compact(LB, L.nB, L.offB, L.boxB, false, ds, ba) : 0;
+  if (lane == 0) {
+    const int la = sub == 0 ? 0 : (sub == 1 ? 3 : 1), lb = sub == 0 ? 5 : (sub == 1 ? 2 : 4);
+    n[la] = nA;
+    n[lb] = nB;
   }
 }
 
@@ -521,8 +509,6 @@ __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds
   __shared__ unsigned long long recK[MODE == 0 ? REC_CAP : 1];
   __shared__ int8_t recT[MODE == 0 ? REC_CAP : 1];
   __shared__ int rec_n, rec_base;
-  __shared__ float sh_box[6 * (NT / 32) + 6];
-  __shared__ int sh_cnt[NT / 32 + 1];
   const int u = blockIdx.x;
   int* n = cnt + 6 * u;
   const int* o = off + 6 * u;
@@ -538,12 +524,7 @@ __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds
   int par = 0;
 #pragma unroll 1
   for (int sub = 0; sub < 3; ++sub) {
-    SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, o, lst, vb, eb, fb);
-    if (L.nA == 0 || L.nB == 0) continue;
-    {
-      const int la = sub == 0 ? 0 : (sub == 1 ? 3 : 1), lb = sub == 0 ? 5 : (sub == 1 ? 2 : 4);
-      refine_lists(L, n + la, n + lb, MODE != 2, ds_f, sh_box, sh_cnt);
-    }
+    SubLists L = sub_lists(g, sub, ovI[u], ovJ[u], n, o, lst, vb, eb, fb);  // lists refined by k_refine
     if (L.nA == 0 || L.nB == 0) continue;
     int cs = 0;
 #pragma unroll 1
@@ -980,6 +961,11 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
     KLAUNCH(K_VG_TOI, s, k_fill_u64<<<nblk(nk, 256), 256, 0, s>>>(cs.toi_key.p, nk, b | 0x8000000000000000ull));
     if (nov > 0) {
       prof_work(K_NARROW_TOI, nov, 48.0 * g.nv);  // positions at q and q + dq
+      KLAUNCH(K_NARROW_TOI, s, k_refine<false><<<nblk(3ll * nov * 32, 256), 256, 0, s>>>(g, ds_f, nov, S.ovI.p,
+                                                                                         S.ovJ.p, cs.bin_cnt.p,
+                                                                                         cs.bin_off.p, cs.lst.p,
+                                                                                         cs.vbox.p, cs.ebox.p,
+                                                                                         cs.fbox.p));
       KLAUNCH(K_NARROW_TOI, s, k_narrow_scan<2><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
                                                                    cs.fbox.p, nullptr, cs.toi_key.p, nullptr, nullptr,
@@ -1009,6 +995,10 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
       cs.stage_key.ensure(1u << 16);
       cs.stage_ty.ensure(1u << 16);
     }
+    KLAUNCH(K_NARROW_SCAN, s, k_refine<true><<<nblk(3ll * nov * 32, 256), 256, 0, s>>>(g, ds_f, nov, S.ovI.p,
+                                                                                       S.ovJ.p, cs.bin_cnt.p,
+                                                                                       cs.bin_off.p, cs.lst.p,
+                                                                                       cs.vbox.p, cs.ebox.p, cs.fbox.p));
     for (int attempt = 0; attempt < 4; ++attempt) {
       CK(cudaMemsetAsync(d_tot + 6, 0, sizeof(int), s));
       KLAUNCH(K_NARROW_SCAN, s, k_narrow_scan<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,

@@ -147,6 +147,9 @@ struct Engine {
     nbufs.Hrow.release(); nbufs.rcol.release(); nbufs.rn.release();
     nbufs.perm.release(); nbufs.cls_cnt.release(); nbufs.cls_off.release(); nbufs.cls_tmp.release();
     nbufs.prec.release();
+    if (nbufs.side) cudaStreamDestroy(nbufs.side);
+    if (nbufs.ev_fork) cudaEventDestroy(nbufs.ev_fork);
+    if (nbufs.ev_join) cudaEventDestroy(nbufs.ev_join);
     nbufs.gpA.release(); nbufs.gpB.release(); nbufs.grp_body.release(); nbufs.grp_n.release();
     nbufs.grp_scene.release(); nbufs.sc_gbeg.release(); nbufs.sc_gend.release(); nbufs.sc_rz.release(); nbufs.sc_bb.release();
     nbufs.sc_conv.release(); nbufs.sc_iters.release(); nbufs.n_active.release();

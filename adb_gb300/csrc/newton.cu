@@ -117,10 +117,11 @@ __device__ __forceinline__ int pair_class(const Geo& g, const Params& P, int kin
 // Per-pair terms, part 1 (kind 0: PT, point on body A, triangle on body B; 1: EE): the
 // barrier's reduced Hessian and gradient, the lagged friction frame and the friction
 // terms, written to the pair's record. Threads take pairs in stencil-class order (perm).
-__global__ void __launch_bounds__(128) k_pair_hess(Geo g, Params P, int kind, int n, const int* tup, const int* perm,
-                                                   double* R, double* lag) {
+__global__ void __launch_bounds__(128) k_pair_hess(Geo g, Params P, int kind, int n, const int* tup,
+                                                   const int8_t* tys, const int* perm, const int* n_moll, double* R,
+                                                   double* lag) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
+  if (t >= n || (n_moll && t < *n_moll)) return;  // mollified pairs: k_pair_moll
   const int p = perm[t];
   int vid[4], na, A, B;
   pair_vertices(g, kind, tup, p, vid, na, A, B);
@@ -131,15 +132,9 @@ __global__ void __launch_bounds__(128) k_pair_hess(Geo g, Params P, int kind, in
     X[i] = ldX(g.X, g.nv, vid[i]);
     X0[i] = ldX(g.X0, g.nv, vid[i]);
   }
-  int ty;
-  double d;
-  if (kind == 0) {
-    ty = pt_type(X[0], X[1], X[2], X[3]);
-    d = pt_dist(X[0], X[1], X[2], X[3], ty);
-  } else {
-    ty = ee_type(X[0], X[1], X[2], X[3]);
-    d = ee_dist(X[0], X[1], X[2], X[3], ty);
-  }
+  // the distance type the cull classified at this same configuration
+  const int ty = tys[p];
+  const double d = kind == 0 ? pt_dist(X[0], X[1], X[2], X[3], ty) : ee_dist(X[0], X[1], X[2], X[3], ty);
   const size_t N = n;
   d3 gv[4];
   FrictionFrame fr;
@@ -187,6 +182,198 @@ __global__ void __launch_bounds__(128) k_pair_hess(Geo g, Params P, int kind, in
   lag[3 * N + p] = fr.c1.x; lag[4 * N + p] = fr.c1.y; lag[5 * N + p] = fr.c1.z;
   for (int i = 0; i < 4; ++i) lag[(6 + i) * N + p] = fr.gam[i];
   lag[10 * N + p] = lam;
+}
+
+// Per-pair terms, part 1 for mollified edge-edge pairs (the first *n_moll entries of
+// perm): one warp per pair. Their 9x9 reduced Hessian has no low-rank structure, so it is
+// built entry by entry across the lanes and projected by a cyclic Jacobi in shared
+// memory whose rotations update the 9 rows in parallel (one lane each); a thread-serial
+// 9x9 Jacobi in local memory kept a few warps busy long after the rest of the launch.
+constexpr int MOLL_W = 4;  // warps (pairs) per CTA
+__global__ void __launch_bounds__(32 * MOLL_W) k_pair_moll(Geo g, Params P, int n, const int* tup,
+                                                           const int8_t* tys, const int* perm, const int* n_moll,
+                                                           double* R, double* lag) {
+  __shared__ double sA[MOLL_W][9][9], sV[MOLL_W][9][9];
+  __shared__ MollData smd[MOLL_W];
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  const int nm = *n_moll;
+  double(&A)[9][9] = sA[wi];
+  double(&V)[9][9] = sV[wi];
+  for (int t = blockIdx.x * MOLL_W + wi; t < nm && t < n; t += gridDim.x * MOLL_W) {
+    const int p = perm[t];
+    int vid[4], na, Ab, Bb;
+    pair_vertices(g, 1, tup, p, vid, na, Ab, Bb);
+    if (!scene_on(g, Ab)) continue;
+    d3 X[4], X0[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      X[i] = ldX(g.X, g.nv, vid[i]);
+      X0[i] = ldX(g.X0, g.nv, vid[i]);
+    }
+    const int ty = tys[p];
+    const double d = ee_dist(X[0], X[1], X[2], X[3], ty);
+    const size_t N = n;
+    const bool active = d < P.dhat;
+    FrictionFrame fr;
+    double lam = 0.0;
+    if (active) {
+      BarrierP bp{P.dhat, P.kappa};
+      frame_ee(X, ty, fr);
+      double uk[2] = {0.0, 0.0};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        d3 du = fsub(X[i], X0[i]);
+        uk[0] += fr.gam[i] * fdot(fr.c0, du);
+        uk[1] += fr.gam[i] * fdot(fr.c1, du);
+      }
+      lam = -barrier_b1(d, bp) * 2 * sqrt(d);
+      Stencil st;
+      d3 w, W[2], gu, gv;
+      double Gi[2][2];
+      MollData md;
+      const bool moll = pair_setup(1, ty, X, d, bp, P.eps_x, st, w, W, Gi, md, gu, gv);
+      if (lane == 0) smd[wi] = md;
+      __syncwarp();
+      // entries of S (upper triangle mirrored), lane e takes e, e + 32, e + 64
+      double orig[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int e = lane + 32 * j;
+        orig[j] = 0.0;
+        if (e < 81) {
+          const int pp = e / 9, qq = e % 9;
+          double h;
+          if (moll) {
+            h = moll_entry(smd[wi], pp <= qq ? pp : qq, pp <= qq ? qq : pp);
+          } else {  // not mollified at this configuration after all: reduced form
+            h = 0.0;
+          }
+          A[pp][qq] = h;
+          V[pp][qq] = pp == qq ? 1.0 : 0.0;
+          orig[j] = h;
+        }
+      }
+      __syncwarp();
+      if (!moll) {
+        // the class test saw a mollified pair but pair_setup does not: the thread path
+        if (lane == 0) {
+          S9Rec rec{R + REC_S * N + p, N};
+          d3 gtmp[4];
+          pair_reduced(1, ty, X, d, bp, P.eps_x, P.psd != 0, rec, gtmp);
+        }
+      } else {
+        bool neg = false;
+        if (P.psd) {
+          for (int sweep = 0; sweep < 30; ++sweep) {
+            double off = 0, tot = 0;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const int e = lane + 32 * j;
+              if (e < 81) {
+                const double v = A[e / 9][e % 9];
+                tot += v * v;
+                if (e / 9 != e % 9) off += v * v;
+              }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+              off += __shfl_xor_sync(0xffffffffu, off, o);
+              tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            }
+            if (off <= 1e-32 * tot || off == 0.0) break;
+            for (int pp = 0; pp < 8; ++pp)
+              for (int qq = pp + 1; qq < 9; ++qq) {
+                const double apq = A[pp][qq];
+                if (apq == 0.0) continue;
+                const double app = A[pp][pp], aqq = A[qq][qq];
+                const double gq = 100.0 * fabs(apq);
+                if (sweep > 2 && fabs(app) + gq == fabs(app) && fabs(aqq) + gq == fabs(aqq)) {
+                  __syncwarp();
+                  if (lane == 0) A[pp][qq] = A[qq][pp] = 0.0;
+                  __syncwarp();
+                  continue;
+                }
+                const double h = 0.5 * (aqq - app);
+                const double den = fabs(h) + sqrt(h * h + apq * apq);
+                const double tt = den > 0.0 ? (h >= 0 ? apq : -apq) / den : 0.0;
+                const double c = rsqrt(1.0 + tt * tt), sn = tt * c;
+                __syncwarp();
+                if (lane < 9 && lane != pp && lane != qq) {
+                  const double akp = A[lane][pp], akq = A[lane][qq];
+                  const double np_ = c * akp - sn * akq, nq = sn * akp + c * akq;
+                  A[lane][pp] = np_;
+                  A[pp][lane] = np_;
+                  A[lane][qq] = nq;
+                  A[qq][lane] = nq;
+                }
+                if (lane < 9) {
+                  const double vkp = V[lane][pp], vkq = V[lane][qq];
+                  V[lane][pp] = c * vkp - sn * vkq;
+                  V[lane][qq] = sn * vkp + c * vkq;
+                }
+                if (lane == 0) {
+                  A[pp][pp] = app - tt * apq;
+                  A[qq][qq] = aqq + tt * apq;
+                  A[pp][qq] = A[qq][pp] = 0.0;
+                }
+                __syncwarp();
+              }
+          }
+#pragma unroll
+          for (int i = 0; i < 9; ++i) neg |= A[i][i] < 0.0;
+        }
+        // S+ = V max(lam, 0) V^T (or S itself when no eigenvalue is negative), upper triangle
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int e = lane + 32 * j;
+          if (e < 81) {
+            const int pp = e / 9, qq = e % 9;
+            if (pp <= qq) {
+              double v = orig[j];
+              if (neg) {
+                v = 0.0;
+                for (int k = 0; k < 9; ++k) {
+                  const double lk = A[k][k];
+                  if (lk > 0) v += V[pp][k] * lk * V[qq][k];
+                }
+              }
+              R[(REC_S + s9_index(pp, qq)) * N + p] = v;
+            }
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        d3 gvv[4];
+        pair_gradient(st, w, md, gu, gv, gvv);
+        if (!(P.terms & TERM_BARRIER)) {
+          for (int k = 0; k < 45; ++k) R[(REC_S + k) * N + p] = 0.0;
+          for (int i = 0; i < 4; ++i) gvv[i] = fd3(0, 0, 0);
+        }
+        double gh[3] = {0, 0, 0}, N6[6] = {0, 0, 0, 0, 0, 0};
+        if (P.ee_fric && (P.terms & TERM_FRICTION)) pair_friction(fr, uk, lam, FrictionP{P.mu, P.epsv, P.max_uk}, gvv, gh, N6);
+        for (int i = 0; i < 4; ++i) {
+          R[(REC_G + 3 * i) * N + p] = gvv[i].x;
+          R[(REC_G + 3 * i + 1) * N + p] = gvv[i].y;
+          R[(REC_G + 3 * i + 2) * N + p] = gvv[i].z;
+        }
+        for (int k = 0; k < 3; ++k) R[(REC_GH + k) * N + p] = gh[k];
+        for (int k = 0; k < 6; ++k) R[(REC_N + k) * N + p] = N6[k];
+      }
+    } else {
+      fr.c0 = fd3(0, 0, 0);
+      fr.c1 = fd3(0, 0, 0);
+      for (int i = 0; i < 4; ++i) fr.gam[i] = 0;
+    }
+    if (lane == 0) {
+      R[REC_ACT * N + p] = active ? 1.0 : 0.0;
+      lag[0 * N + p] = fr.c0.x; lag[1 * N + p] = fr.c0.y; lag[2 * N + p] = fr.c0.z;
+      lag[3 * N + p] = fr.c1.x; lag[4 * N + p] = fr.c1.y; lag[5 * N + p] = fr.c1.z;
+      for (int i = 0; i < 4; ++i) lag[(6 + i) * N + p] = fr.gam[i];
+      lag[10 * N + p] = lam;
+    }
+    __syncwarp();
+  }
 }
 
 // Per-pair terms, part 2: the chain rule onto the 12 affine DOFs of the two bodies,
@@ -977,6 +1164,7 @@ struct EnergyArgs {
   double alpha;  // used when the geometry carries no per-scene step
   int with_bi;
   const int *pt, *ee, *vg, *lpt_t, *lee_t, *lvg_t;
+  const int8_t *pt_ty, *ee_ty;  // distance types classified by the cull at this configuration
   const double *lpt_lag, *lee_lag, *lvg_lam;
   const int* off;        // NSEG * (ns + 1): first element of each scene in each list
   const int* chunk_off;  // ns + 1
@@ -1031,8 +1219,7 @@ __device__ double energy_term(const Geo& g, const Params& P, const EnergyArgs& a
     pair_vids(g, 0, a.pt, i, vid);
     d3 X0 = ldX(g.X, g.nv, vid[0]), X1 = ldX(g.X, g.nv, vid[1]), X2 = ldX(g.X, g.nv, vid[2]),
        X3 = ldX(g.X, g.nv, vid[3]);
-    int ty = pt_type(X0, X1, X2, X3);
-    return barrier_b(pt_dist(X0, X1, X2, X3, ty), bp);
+    return barrier_b(pt_dist(X0, X1, X2, X3, a.pt_ty[i]), bp);
   }
   if (seg == SEG_EE) {
     if (!P.ee) return 0.0;
@@ -1049,8 +1236,7 @@ __device__ double energy_term(const Geo& g, const Params& P, const EnergyArgs& a
       double xe = x / eps_x;
       m = (-xe + 2.0) * xe;
     }
-    int ty = ee_type(X0, X1, X2, X3);
-    return barrier_b(ee_dist(X0, X1, X2, X3, ty), bp) * m;
+    return barrier_b(ee_dist(X0, X1, X2, X3, a.ee_ty[i]), bp) * m;
   }
   if (seg == SEG_VG) {
     if (!P.ground) return 0.0;
@@ -1343,8 +1529,26 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
     scan_exclusive_int(B.cls_cnt.p, B.cls_off.p, NCLS * nb_c, nullptr, s, B.cls_tmp);
     KLAUNCH(K_SEG, s, k_class_scatter<<<nb_c, CLS_T, 0, s>>>(g, P, kind, n, tup, ty, B.cls_off.p, B.perm.p));
     B.prec.ensure(REC * (size_t)n);
-    KLAUNCH(K_PAIR_TERMS, s, k_pair_hess<<<nblk(n, 128), 128, 0, s>>>(g, P, kind, n, tup, B.perm.p, B.prec.p,
-                                                                    kind ? S.ee_lag.p : S.pt_lag.p));
+    // class 0 (mollified edge-edge pairs) comes first in perm; its size is the offset of
+    // class 1
+    const int* n_moll = kind ? B.cls_off.p + nb_c : nullptr;
+    if (kind) {
+      // the few mollified pairs take one warp each for a long serial projection: run
+      // them on a side stream, overlapped with the main kernel
+      if (!B.side) {
+        CK(cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&B.ev_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&B.ev_join, cudaEventDisableTiming));
+      }
+      CK(cudaEventRecord(B.ev_fork, s));
+      CK(cudaStreamWaitEvent(B.side, B.ev_fork, 0));
+      KLAUNCH(K_PAIR_TERMS, B.side, k_pair_moll<<<64, 32 * MOLL_W, 0, B.side>>>(g, P, n, tup, ty, B.perm.p, n_moll,
+                                                                              B.prec.p, S.ee_lag.p));
+      CK(cudaEventRecord(B.ev_join, B.side));
+    }
+    KLAUNCH(K_PAIR_TERMS, s, k_pair_hess<<<nblk(n, 128), 128, 0, s>>>(g, P, kind, n, tup, ty, B.perm.p, n_moll,
+                                                                    B.prec.p, kind ? S.ee_lag.p : S.pt_lag.p));
+    if (kind) CK(cudaStreamWaitEvent(s, B.ev_join, 0));
     KLAUNCH(K_PAIR_TERMS, s, k_pair_chain<<<nblk(n, 128), 128, 0, s>>>(g, kind, n, tup, kind ? S.ee_ov.p : S.pt_ov.p,
                                                                      S.ovI.p, B.prec.p,
                                                                      kind ? B.ee_c.p : B.pt_c.p));
@@ -1481,6 +1685,8 @@ void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet&
   a.with_bi = with_bi ? 1 : 0;
   a.pt = Snew.pt.p;
   a.ee = Snew.ee.p;
+  a.pt_ty = Snew.pt_ty.p;
+  a.ee_ty = Snew.ee_ty.p;
   a.vg = Snew.vg.p;
   a.lpt_t = Slag.pt.p;
   a.lee_t = Slag.ee.p;
