@@ -104,6 +104,7 @@ struct CullScratch {
   DBuf<double> ovcull;
   DBuf<float> ovcull_f;
   DBuf<float> vbox, ebox, fbox;
+  DBuf<int> order, order_cnt;           // narrow-phase processing order of the overlaps
   DBuf<int> bin_cnt, bin_off, lst;
   DBuf<long long> cand_cnt, cand_off;
   DBuf<uint8_t> flags;

@@ -134,6 +134,7 @@ struct Engine {
     }
     cs.bbox.release(); cs.cnt_all.release(); cs.cnt_up.release(); cs.up_ptr.release(); cs.rowid.release();
     cs.ovcull.release(); cs.ovcull_f.release(); cs.vbox.release(); cs.ebox.release(); cs.fbox.release();
+    cs.order.release(); cs.order_cnt.release();
     cs.bin_cnt.release(); cs.bin_off.release(); cs.lst.release(); cs.cand_cnt.release(); cs.cand_off.release();
     cs.flags.release(); cs.blk_a.release(); cs.blk_b.release(); cs.blk_a_off.release(); cs.blk_b_off.release();
     cs.vflag_cnt.release(); cs.vflag_off.release(); cs.sub_cnt.release(); cs.stage_off.release();
