@@ -4,8 +4,9 @@
 ``ABD.implicit_euler`` and returns the final ``(q, v)``; gradients with respect to the
 initial state, the initial velocities and the friction coefficient come from the adjoint
 of each converged frame (``abd_adjoint_frame``: implicit differentiation, solved by the
-same block-sparse PCG). Forward states are kept every ``every`` frames; the backward pass
-recomputes each segment from its checkpoint and walks it in reverse. The frame's velocity
+same block-sparse PCG). Forward states are kept every ``every`` frames (every frame by
+default: a state is 24 doubles per body); the backward pass recomputes the frames between
+checkpoints from the one before them and walks each segment in reverse. The frame's velocity
 update v_{t+1} = (q_{t+1} - q_t) / dt (model/abd.cpp:128-139) is differentiated here.
 
 The adjoint system uses the exact Hessian (no PSD projection, the ground barrier's full
@@ -37,6 +38,7 @@ class Rollout(torch.autograd.Function):
             if (t + 1) % every == 0 and t + 1 < n_steps:
                 ckpt[t + 1] = sim.state()
         qT, vT = sim.state()
+        ckpt[n_steps] = (qT.copy(), vT.copy())
         ctx.sim, ctx.n, ctx.ckpt = sim, n_steps, ckpt
         return torch.from_numpy(qT.copy()), torch.from_numpy(vT.copy())
 
@@ -49,12 +51,20 @@ class Rollout(torch.autograd.Function):
         gv = np.zeros(shape) if gvT is None else gvT.detach().cpu().numpy().astype(np.float64).copy()
         gmu = 0.0
         t_end = n
-        for s0 in sorted(ckpt, reverse=True):
+        for s0 in sorted((k for k in ckpt if k < n), reverse=True):
+            # states s0 .. t_end of the segment: stored ones are reused, the rest recomputed
             states = [ckpt[s0]]
-            sim.set_state(*ckpt[s0])
-            for _ in range(s0, t_end):
+            stepped = False
+            for t in range(s0, t_end):
+                if t + 1 in ckpt:
+                    states.append(ckpt[t + 1])
+                    stepped = False
+                    continue
+                if not stepped:
+                    sim.set_state(*states[-1])
                 sim.step(1)
                 states.append(sim.state())
+                stepped = True
             for t in range(t_end - 1, s0 - 1, -1):
                 (q_t, v_t), (q_n, _) = states[t - s0], states[t - s0 + 1]
                 # v_{t+1} = (q_{t+1} - q_t) / dt
@@ -66,7 +76,7 @@ class Rollout(torch.autograd.Function):
         return torch.from_numpy(gq), torch.from_numpy(gv), torch.tensor(gmu, dtype=torch.float64), None, None, None
 
 
-def rollout(sim: ABD, q0, v0, mu, n_steps: int, every: int = 10):
+def rollout(sim: ABD, q0, v0, mu, n_steps: int, every: int = 1):
     """Differentiable (q_T, v_T) after n_steps frames from (q0, v0) with friction mu."""
     mu = mu if torch.is_tensor(mu) else torch.tensor(float(mu), dtype=torch.float64)
     return Rollout.apply(q0, v0, mu, sim, int(n_steps), int(every))

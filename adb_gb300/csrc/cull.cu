@@ -265,22 +265,39 @@ __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const 
     else { beg = g.f_off[body]; end = g.f_off[body + 1]; fbx = fb; }
     int slot = u * 6 + side * 3 + kind;
     int c = 0, base = pass != BIN_COUNT ? off[slot] : 0;
-    for (int k0 = beg; k0 < end; k0 += 32) {
-      int k = k0 + lane;
-      bool hit = false;
-      if (k < end) {
-        const float* q = fbx + 6 * k;
-        if (f_overlap(cf, q)) {
-          hit = q[0] < ci[3] && q[1] < ci[4] && q[2] < ci[5] && q[3] > ci[0] && q[4] > ci[1] && q[5] > ci[2];
+    // BIN_R runs of 32 per step: their boxes are loaded before any is tested, so the
+    // warp keeps several L2 loads in flight
+    constexpr int BIN_R = 4;
+    for (int k0 = beg; k0 < end; k0 += 32 * BIN_R) {
+      float q[BIN_R][6];
+#pragma unroll
+      for (int r = 0; r < BIN_R; ++r) {
+        const int k = k0 + 32 * r + lane;
+        if (k < end) {
+          const float2* src = reinterpret_cast<const float2*>(fbx + 6 * (size_t)k);
+          float2 a = src[0], b = src[1], d = src[2];
+          q[r][0] = a.x; q[r][1] = a.y; q[r][2] = b.x; q[r][3] = b.y; q[r][4] = d.x; q[r][5] = d.y;
+        } else {
+          q[r][0] = q[r][1] = q[r][2] = INFINITY;  // misses every box
+          q[r][3] = q[r][4] = q[r][5] = -INFINITY;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < BIN_R; ++r) {
+        const int k = k0 + 32 * r + lane;
+        bool hit = false;
+        if (f_overlap(cf, q[r])) {
+          hit = q[r][0] < ci[3] && q[r][1] < ci[4] && q[r][2] < ci[5] && q[r][3] > ci[0] && q[r][4] > ci[1] &&
+                q[r][5] > ci[2];
           if (!hit) {
             box b = (kind == 0) ? vbox_exact(g, k, traj) : (kind == 1 ? ebox_exact(g, k, traj) : fbox_exact(g, k, traj));
             hit = overlaps(cull, b);
           }
         }
+        unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (pass != BIN_COUNT && hit) lst[base + c + __popc(m & below)] = k - beg;
+        c += __popc(m);
       }
-      unsigned m = __ballot_sync(0xffffffffu, hit);
-      if (pass != BIN_COUNT && hit) lst[base + c + __popc(m & below)] = k - beg;
-      c += __popc(m);
     }
     if (pass != BIN_WRITE && lane == 0) cnt[slot] = c;
   }

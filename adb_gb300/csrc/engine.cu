@@ -901,7 +901,7 @@ int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const
         dn += (w[k] - wprev[k]) * (w[k] - wprev[k]);
         wn += w[k] * w[k];
       }
-      if (it > 0 && dn <= 1e-28 * wn) break;
+      if (it > 0 && dn <= 1e-24 * wn) break;  // w settled to ~1e-12 relative
       abd::vg_lag_adjoint(g, Pe, S, e.nbufs.x.p, e.nbufs.qv.p, e.s);  // PCG scratch between solves
       CK(cudaMemcpyAsync(ctw.data(), e.nbufs.qv.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
       CK(cudaStreamSynchronize(e.s));
