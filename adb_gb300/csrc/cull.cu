@@ -304,10 +304,10 @@ __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const 
 }
 
 constexpr int NT = 256;     // narrow-phase threads per CTA
-constexpr int TILE = 384;   // primitives of one list staged in shared memory (2 x 9 kB)
+constexpr int TILE = 256;   // primitives of one list staged in shared memory (2 x 6 kB)
 constexpr int REC_CAP = 2048;  // accepted pairs of one overlap kept in shared memory for sorting
-constexpr int STEP = 8;     // box-phase candidates per thread between two exact phases
-constexpr int QCAP = NT * STEP;  // queue of float-box hits (8 kB)
+constexpr int STEP = 16;    // box-phase candidates per thread between two exact phases
+constexpr int QCAP = NT * STEP;  // queue of float-box hits (16 kB)
 
 __device__ __forceinline__ void finflate(const float* s, float ds, float* o) {
   o[0] = __fsub_rd(s[0], ds); o[1] = __fsub_rd(s[1], ds); o[2] = __fsub_rd(s[2], ds);
@@ -340,6 +340,149 @@ __device__ __forceinline__ int exact_pair(const Geo& g, const Params& P, int sub
   if (lb_reject_ee(a0, a1, b0, b1, P.dhat)) return 0;
   int ty = ee_type(a0, a1, b0, b1);
   return (ee_dist(a0, a1, b0, b1, ty) < P.dhat) ? 1 + ty : 0;
+}
+
+// ---- FP32 lower bounds of pair distances with tracked rounding errors ----
+// A value v carries a bound e on |v - exact|, where "exact" is the same expression in real
+// arithmetic on the FP64 positions. Inputs are the lower corners of the vertex float
+// boxes (rd(x), |x - rd(x)| <= 2^-23 |x|); every operation adds its rounding (u |v| with
+// u = 2^-24, slightly enlarged, plus an underflow term), and the error terms themselves
+// are accumulated rounding up. The bounds are therefore rigorous; they let most float-box
+// hits be rejected without the FP64 test (GB300 issues FP64 at 1/64 of the FP32 rate).
+struct EF {
+  float v, e;
+};
+__device__ __forceinline__ EF ef_in(float x) { return {x, __fadd_ru(__fmul_ru(fabsf(x), 1.2042e-7f), 1e-37f)}; }
+__device__ __forceinline__ float ef_rnd(float v) { return __fadd_ru(__fmul_ru(fabsf(v), 6.0e-8f), 1e-37f); }
+__device__ __forceinline__ EF ef_add(EF a, EF b) {
+  const float v = __fadd_rn(a.v, b.v);
+  return {v, __fadd_ru(__fadd_ru(a.e, b.e), ef_rnd(v))};
+}
+__device__ __forceinline__ EF ef_sub(EF a, EF b) {
+  const float v = __fsub_rn(a.v, b.v);
+  return {v, __fadd_ru(__fadd_ru(a.e, b.e), ef_rnd(v))};
+}
+__device__ __forceinline__ EF ef_mul(EF a, EF b) {
+  const float v = __fmul_rn(a.v, b.v);
+  float e = __fadd_ru(__fmul_ru(fabsf(a.v), b.e), __fmul_ru(fabsf(b.v), a.e));
+  e = __fadd_ru(e, __fmul_ru(a.e, b.e));
+  return {v, __fadd_ru(e, ef_rnd(v))};
+}
+struct EF3 {
+  EF x[3];
+};
+__device__ __forceinline__ EF3 ef3_in(const float* p) { return {{ef_in(p[0]), ef_in(p[1]), ef_in(p[2])}}; }
+__device__ __forceinline__ EF3 ef3_sub(const EF3& a, const EF3& b) {
+  return {{ef_sub(a.x[0], b.x[0]), ef_sub(a.x[1], b.x[1]), ef_sub(a.x[2], b.x[2])}};
+}
+__device__ __forceinline__ EF3 ef3_cross(const EF3& a, const EF3& b) {
+  return {{ef_sub(ef_mul(a.x[1], b.x[2]), ef_mul(a.x[2], b.x[1])),
+           ef_sub(ef_mul(a.x[2], b.x[0]), ef_mul(a.x[0], b.x[2])),
+           ef_sub(ef_mul(a.x[0], b.x[1]), ef_mul(a.x[1], b.x[0]))}};
+}
+__device__ __forceinline__ EF ef3_dot(const EF3& a, const EF3& b) {
+  return ef_add(ef_add(ef_mul(a.x[0], b.x[0]), ef_mul(a.x[1], b.x[1])), ef_mul(a.x[2], b.x[2]));
+}
+// lower bound of num^2 / den for num known positive by at least lo > 0, den <= den.v + den.e
+__device__ __forceinline__ float ef_ratio_lb(float lo, EF den) {
+  return __fdiv_rd(__fmul_rd(lo, lo), __fadd_ru(den.v, den.e));
+}
+// lower bound of |x| (0 when the sign is not certain)
+__device__ __forceinline__ float ef_abs_lb(EF x) { return fmaxf(__fsub_rd(fabsf(x.v), x.e), 0.f); }
+
+// Lower bound of the squared point-triangle distance: the point-plane distance combined
+// with the largest distance of the point beyond one of the triangle's edge lines in the
+// plane (the two components are orthogonal).
+__device__ __forceinline__ float lb2_pt_f(const float* p, const float* t0, const float* t1, const float* t2) {
+  const EF3 P = ef3_in(p), T0 = ef3_in(t0), T1 = ef3_in(t1), T2 = ef3_in(t2);
+  const EF3 e1 = ef3_sub(T1, T0), e2 = ef3_sub(T2, T0), e3 = ef3_sub(T2, T1), w = ef3_sub(P, T0);
+  const EF3 n = ef3_cross(e1, e2);
+  const EF nn = ef3_dot(n, n);
+  const float sl = ef_abs_lb(ef3_dot(w, n));
+  float lb = sl > 0.f ? ef_ratio_lb(sl, nn) : 0.f;
+  // outward in-plane edge normals m = edge x n (edges t0->t1, t1->t2, t2->t0)
+  const EF3 me[3] = {ef3_cross(e1, n), ef3_cross(e3, n), ef3_cross(ef3_sub(T0, T2), n)};
+  const EF3 ve[3] = {w, ef3_sub(P, T1), ef3_sub(P, T2)};
+  float side = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const EF num = ef3_dot(ve[k], me[k]);
+    const float lo = __fsub_rd(num.v, num.e);
+    if (lo > 0.f) side = fmaxf(side, ef_ratio_lb(lo, ef3_dot(me[k], me[k])));
+  }
+  return __fadd_rd(lb, side);
+}
+
+// Lower bound of the squared segment-segment distance: the line-line distance combined
+// with one in-plane separation: one segment entirely on one side of the other's line, or
+// beyond one of its ends along its direction.
+__device__ __forceinline__ float lb2_ee_f(const float* a0, const float* a1, const float* b0, const float* b1) {
+  const EF3 A0 = ef3_in(a0), A1 = ef3_in(a1), B0 = ef3_in(b0), B1 = ef3_in(b1);
+  const EF3 u = ef3_sub(A1, A0), v = ef3_sub(B1, B0);
+  const EF3 n = ef3_cross(u, v);
+  const EF nn = ef3_dot(n, n);
+  const float sl = ef_abs_lb(ef3_dot(ef3_sub(B0, A0), n));
+  float lb = sl > 0.f ? ef_ratio_lb(sl, nn) : 0.f;
+  float sep = 0.f;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const EF3& d = k == 0 ? u : v;
+    const EF3& base = k == 0 ? A0 : B0;
+    const EF3 q0 = ef3_sub(k == 0 ? B0 : A0, base), q1 = ef3_sub(k == 0 ? B1 : A1, base);
+    // the other segment on one side of this one's line (in-plane normal n x d)
+    const EF3 m = ef3_cross(n, d);
+    const EF x0 = ef3_dot(q0, m), x1 = ef3_dot(q1, m);
+    float lo = 0.f;
+    if (__fsub_rd(x0.v, x0.e) > 0.f && __fsub_rd(x1.v, x1.e) > 0.f)
+      lo = fminf(__fsub_rd(x0.v, x0.e), __fsub_rd(x1.v, x1.e));
+    else if (__fadd_ru(x0.v, x0.e) < 0.f && __fadd_ru(x1.v, x1.e) < 0.f)
+      lo = fminf(-__fadd_ru(x0.v, x0.e), -__fadd_ru(x1.v, x1.e));
+    if (lo > 0.f) sep = fmaxf(sep, ef_ratio_lb(lo, ef3_dot(m, m)));
+    // the other segment beyond one end of this one along d
+    const EF dd = ef3_dot(d, d);
+    const EF y0 = ef3_dot(q0, d), y1 = ef3_dot(q1, d);
+    const EF z0 = ef_sub(y0, dd), z1 = ef_sub(y1, dd);
+    lo = 0.f;
+    if (__fsub_rd(z0.v, z0.e) > 0.f && __fsub_rd(z1.v, z1.e) > 0.f)
+      lo = fminf(__fsub_rd(z0.v, z0.e), __fsub_rd(z1.v, z1.e));
+    else if (__fadd_ru(y0.v, y0.e) < 0.f && __fadd_ru(y1.v, y1.e) < 0.f)
+      lo = fminf(-__fadd_ru(y0.v, y0.e), -__fadd_ru(y1.v, y1.e));
+    if (lo > 0.f) sep = fmaxf(sep, ef_ratio_lb(lo, dd));
+  }
+  return __fadd_rd(lb, sep);
+}
+
+// Rejects a float-box hit when the float lower bound of its squared distance reaches
+// dhat (1 + 1e-4) and the primitive is well shaped (the guards of lb_reject_pt/ee, so
+// the FP64 distance is accurate there): such a pair is one the FP64 test rejects too.
+__device__ __forceinline__ bool f_reject(const Geo& g, const float* vb, int sub, int pa, int pb, float lim) {
+  const float *x0, *x1, *x2, *x3;
+  if (sub < 2) {
+    const int* f = g.fv + 3 * pb;
+    x0 = vb + 6 * pa; x1 = vb + 6 * f[0]; x2 = vb + 6 * f[1]; x3 = vb + 6 * f[2];
+  } else {
+    const int* ea = g.ev + 2 * pa;
+    const int* eb = g.ev + 2 * pb;
+    x0 = vb + 6 * ea[0]; x1 = vb + 6 * ea[1]; x2 = vb + 6 * eb[0]; x3 = vb + 6 * eb[1];
+  }
+  // well-shaped guards in plain float with twice the FP64 guards' margins
+  float ea[3], eb[3];
+  for (int c = 0; c < 3; ++c) {
+    ea[c] = sub < 2 ? x2[c] - x1[c] : x1[c] - x0[c];
+    eb[c] = sub < 2 ? x3[c] - x1[c] : x3[c] - x2[c];
+  }
+  const float la = ea[0] * ea[0] + ea[1] * ea[1] + ea[2] * ea[2];
+  const float lb = eb[0] * eb[0] + eb[1] * eb[1] + eb[2] * eb[2];
+  const float nx = ea[1] * eb[2] - ea[2] * eb[1], ny = ea[2] * eb[0] - ea[0] * eb[2], nz = ea[0] * eb[1] - ea[1] * eb[0];
+  const float nn = nx * nx + ny * ny + nz * nz;
+  float lmin = fminf(la, lb);
+  if (sub < 2) {
+    const float d0 = x3[0] - x2[0], d1 = x3[1] - x2[1], d2 = x3[2] - x2[2];
+    lmin = fminf(lmin, d0 * d0 + d1 * d1 + d2 * d2);
+  }
+  if (!(lmin >= 2e-6f * lim) || !(nn >= 2e-6f * la * lb)) return false;
+  const float l2 = sub < 2 ? lb2_pt_f(x0, x1, x2, x3) : lb2_ee_f(x0, x1, x2, x3);
+  return l2 >= lim;
 }
 
 // Trajectory time of impact of one candidate (vtn 3), exact box test included.
@@ -549,6 +692,7 @@ __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds
   __shared__ int8_t recT[MODE == 0 ? REC_CAP : 1];
   __shared__ int rec_n, rec_base;
   const int u = order[blockIdx.x];
+  const float lim_f = __double2float_ru(P.dhat * (1.0 + 1e-4));
   int* n = cnt + 6 * u;
   const int* o = off + 6 * u;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -628,7 +772,7 @@ __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds
             if (MODE == 2) {
               tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
             } else {
-              int f = exact_pair(g, P, sub, pa, pb);
+              int f = f_reject(g, vb, sub, pa, pb, lim_f) ? 0 : exact_pair(g, P, sub, pa, pb);
               if (f) {
                 ++cs;
                 int slot = atomicAdd(&rec_n, 1);

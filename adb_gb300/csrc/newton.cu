@@ -743,6 +743,7 @@ constexpr int NPART = 4;                 // 16-lane groups per body in the produ
 constexpr int BODY_SLOTS = 16 * NPART;   // threads per body
 constexpr int GB = 8;                    // bodies per group
 constexpr int PCG_NT = GB * BODY_SLOTS;  // threads per CTA
+constexpr int PCG_CACHE = 16;            // loop steps whose scene scalars a CTA keeps on chip
 
 struct PcgArgs {
   int nb, ns, ngrp;
@@ -923,6 +924,10 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
   __shared__ double s_sum[2];
   __shared__ double s_val;   // alpha or beta of this CTA's scene
   __shared__ int s_flag;     // 1: this CTA's scene does no work in this phase
+  // the scalars this CTA computed for the scene of loop step it < PCG_CACHE (the global
+  // copies, written by the scene's owner CTA, serve the later steps)
+  __shared__ double s_c_rz[PCG_CACHE], s_c_bb[PCG_CACHE];
+  __shared__ int s_c_conv[PCG_CACHE];
   const int nloop = (a.ngrp + gridDim.x - 1) / gridDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1003,11 +1008,20 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
         int was_conv = 0, on = 1;
         double bb = 0.0, rzp = 1.0;
         if (threadIdx.x == 0) {
-          was_conv = k > 0 ? conv_prev[sc] : 0;
-          on = a.sc_on[sc];
-          if (k > 0) {
-            bb = a.sc_bb[sc];
-            rzp = rz_prev[sc];
+          if (it < PCG_CACHE) {  // this CTA's own values from the previous iteration
+            was_conv = k > 0 ? s_c_conv[it] : 0;
+            on = k > 0 ? 1 : a.sc_on[sc];
+            if (k > 0) {
+              bb = s_c_bb[it];
+              rzp = s_c_rz[it];
+            }
+          } else {
+            was_conv = k > 0 ? conv_prev[sc] : 0;
+            on = a.sc_on[sc];
+            if (k > 0) {
+              bb = a.sc_bb[sc];
+              rzp = rz_prev[sc];
+            }
           }
         }
         if (warp < 2) {
@@ -1026,11 +1040,16 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
             if (k == 0) {
               conv = !on || rr == 0.0;
               if (owner) a.sc_bb[sc] = rr;
+              if (it < PCG_CACHE) s_c_bb[it] = rr;
             } else {
               conv = !(rr > a.tol2 * bb);
             }
             s_val = k == 0 ? 0.0 : rz / rzp;
             s_flag = conv || k == a.maxit;
+            if (it < PCG_CACHE) {
+              s_c_conv[it] = conv ? 1 : 0;
+              s_c_rz[it] = rz;
+            }
             if (owner) {
               rz_cur[sc] = rz;
               conv_cur[sc] = conv ? 1 : 0;
@@ -1100,9 +1119,9 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
     for (int it = 0; it < nloop; ++it) {
       int g, sc, b0, nbody;
       group(it, g, sc, b0, nbody);
-      const bool act = g >= 0 && !conv_cur[sc];
+      const bool act = g >= 0 && !(it < PCG_CACHE ? s_c_conv[it] : conv_cur[sc]);
       if (act && warp == 0) {
-        const double rz = lane == 0 ? rz_cur[sc] : 0.0;
+        const double rz = lane == 0 ? (it < PCG_CACHE ? s_c_rz[it] : rz_cur[sc]) : 0.0;
         const double pq = warp_scene_sum(a.gpA, 0, a.sc_gbeg[sc], a.sc_gend[sc]);
         if (lane == 0) s_val = rz / pq;
       }
