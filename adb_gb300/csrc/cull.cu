@@ -304,10 +304,15 @@ __global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const 
 }
 
 constexpr int NT = 256;     // narrow-phase threads per CTA
-constexpr int TILE = 256;   // primitives of one list staged in shared memory (2 x 6 kB)
+constexpr int TILE = 384;   // primitives of one list staged in shared memory (2 x 9 kB)
 constexpr int REC_CAP = 2048;  // accepted pairs of one overlap kept in shared memory for sorting
-constexpr int STEP = 16;    // box-phase candidates per thread between two exact phases
-constexpr int QCAP = NT * STEP;  // queue of float-box hits (16 kB)
+constexpr int STEP = 64;    // box-phase candidates per thread between two exact phases
+constexpr int QCAP = NT * STEP;  // queue of float-box hits (64 kB)
+// dynamic shared memory of k_narrow_scan<MODE>: boxes, queue, accepted pairs (MODE 0)
+__host__ __device__ constexpr size_t narrow_smem(int mode) {
+  return 2 * TILE * 6 * sizeof(float) + QCAP * sizeof(unsigned) +
+         (mode == 0 ? REC_CAP * (sizeof(unsigned long long) + 1) : 0);
+}
 
 __device__ __forceinline__ void finflate(const float* s, float ds, float* o) {
   o[0] = __fsub_rd(s[0], ds); o[1] = __fsub_rd(s[1], ds); o[2] = __fsub_rd(s[2], ds);
@@ -685,11 +690,13 @@ __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds
                                                     unsigned long long* toi_key, unsigned long long* stage_key,
                                                     int8_t* stage_ty, int* stage_off, int* stage_total,
                                                     int stage_cap, const int* order) {
-  __shared__ float sA[TILE * 6], sB[TILE * 6];
-  __shared__ unsigned int sq[QCAP];
+  extern __shared__ __align__(16) unsigned char smem_dyn[];
+  unsigned long long* recK = reinterpret_cast<unsigned long long*>(smem_dyn);  // REC_CAP (MODE 0)
+  float* sA = reinterpret_cast<float*>(smem_dyn + (MODE == 0 ? REC_CAP * sizeof(unsigned long long) : 0));
+  float* sB = sA + TILE * 6;
+  unsigned int* sq = reinterpret_cast<unsigned int*>(sB + TILE * 6);
+  int8_t* recT = reinterpret_cast<int8_t*>(sq + QCAP);                         // REC_CAP (MODE 0)
   __shared__ int sq_n[2];
-  __shared__ unsigned long long recK[MODE == 0 ? REC_CAP : 1];
-  __shared__ int8_t recT[MODE == 0 ? REC_CAP : 1];
   __shared__ int rec_n, rec_base;
   const int u = order[blockIdx.x];
   const float lim_f = __double2float_ru(P.dhat * (1.0 + 1e-4));
@@ -1029,6 +1036,18 @@ __global__ void k_fill_u64(unsigned long long* p, int n, unsigned long long v) {
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 // Smallest float >= d (host side).
+// Lets the narrow-phase CTAs use more than the default 48 kB of shared memory (once per
+// device; the setting is part of this process's context only).
+static void narrow_smem_attr() {
+  static int done_dev = -1;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (done_dev == dev) return;
+  CK(cudaFuncSetAttribute(k_narrow_scan<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(0)));
+  CK(cudaFuncSetAttribute(k_narrow_scan<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(2)));
+  done_dev = dev;
+}
+
 // Fills cs.order with the overlaps heaviest bucket first (k_order_count / k_order_place).
 static void order_overlaps(int nov, CullScratch& cs, cudaStream_t s, int tag) {
   cs.order.ensure(nov + 1);
@@ -1159,7 +1178,8 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
                                                                                          cs.vbox.p, cs.ebox.p,
                                                                                          cs.fbox.p));
       order_overlaps(nov, cs, s, K_NARROW_TOI);
-      KLAUNCH(K_NARROW_TOI, s, k_narrow_scan<2><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
+      narrow_smem_attr();
+      KLAUNCH(K_NARROW_TOI, s, k_narrow_scan<2><<<nov, NT, narrow_smem(2), s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
                                                                    cs.fbox.p, nullptr, cs.toi_key.p, nullptr, nullptr,
                                                                    nullptr, nullptr, 0, cs.order.p));
@@ -1195,7 +1215,8 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
     order_overlaps(nov, cs, s, K_NARROW_SCAN);
     for (int attempt = 0; attempt < 4; ++attempt) {
       CK(cudaMemsetAsync(d_tot + 6, 0, sizeof(int), s));
-      KLAUNCH(K_NARROW_SCAN, s, k_narrow_scan<0><<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
+      narrow_smem_attr();
+      KLAUNCH(K_NARROW_SCAN, s, k_narrow_scan<0><<<nov, NT, narrow_smem(0), s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
                                                                       cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
                                                                       cs.fbox.p, cs.sub_cnt.p, nullptr, cs.stage_key.p,
                                                                       cs.stage_ty.p, cs.stage_off.p, d_tot + 6,

@@ -845,7 +845,17 @@ __global__ void k_pcg_rows(int nb, const int* row_ptr, const int* col, const int
 // over all warps costs far more than one warp doing it.)
 __device__ __forceinline__ double warp_scene_sum(const double* v, int comp, int beg, int end) {
   double s = 0.0;
-  for (int k = beg + (int)(threadIdx.x & 31); k < end; k += 32) s += v[2 * k + comp];
+  int k = beg + (int)(threadIdx.x & 31);
+  // four loads in flight before the adds (same order of additions)
+  for (; k + 96 < end; k += 128) {
+    const double a = v[2 * k + comp], b = v[2 * (k + 32) + comp], c = v[2 * (k + 64) + comp],
+                 d = v[2 * (k + 96) + comp];
+    s += a;
+    s += b;
+    s += c;
+    s += d;
+  }
+  for (; k < end; k += 32) s += v[2 * k + comp];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
@@ -1164,6 +1174,236 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg(PcgArgs a) {
       const int idx = 12 * (b0 + vlb) + row;
       a.dq[idx] = -a.x[idx];
     }
+  }
+  if (tid == 0) a.out[1] = k;
+}
+
+// The same solve when every CTA holds exactly one body group (grid = groups, the common
+// case up to 152 groups per cooperative launch): each thread keeps its row's x, r, z, p
+// and q, its row of the block-Jacobi inverse and its first two row blocks of the product
+// in registers for the whole solve, and z = M^-1 r takes the body's r from its 16-lane
+// half by shuffles. Only the neighbour reads of z and p and the group partials go through
+// memory. The arithmetic is that of k_pcg, operation for operation, so both give the same
+// iterates bit for bit.
+constexpr int PCG1_NC = 2;  // row blocks per part kept in registers
+__global__ void __launch_bounds__(PCG_NT) k_pcg1(PcgArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ double s_part[PCG_NT];
+  __shared__ double s_w[GB];
+  __shared__ __align__(16) double s_v[PCG_NT / 16][12];
+  __shared__ double s_sum[2];
+  __shared__ double s_val;
+  __shared__ int s_flag;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int part = (threadIdx.x >> 4) & (NPART - 1), prow = threadIdx.x & 15;
+  const int plb = threadIdx.x / BODY_SLOTS;
+  const int hg = threadIdx.x >> 4;
+  const bool vthr = threadIdx.x < 16 * GB;
+  const int vlb = threadIdx.x >> 4, row = threadIdx.x & 15;
+  const int g = blockIdx.x;
+  const int sc = a.grp_scene[g], nbody = a.grp_n[g], b0 = a.grp_body[g];
+  const bool owner = g == a.sc_gbeg[sc];
+  // product-phase state
+  const bool pact = plb < nbody;
+  const int pbody = b0 + plb;
+  const int pbase = pact ? pbody + a.row_ptr[pbody] : 0, pn = pact ? a.rn[pbody] : 0;
+  int rc[PCG1_NC];
+  double hr[PCG1_NC][12];
+#pragma unroll
+  for (int jj = 0; jj < PCG1_NC; ++jj) {
+    const int j = part + NPART * jj;
+    rc[jj] = j < pn ? a.rcol[pbase + j] : 0;
+#pragma unroll
+    for (int c = 0; c < 12; ++c) hr[jj][c] = (j < pn && prow < 12) ? a.Hrow[(size_t)(pbase + j) * 144 + 12 * prow + c] : 0.0;
+  }
+  // per-row state
+  const bool mine = vthr && vlb < nbody && row < 12;
+  const int vbody = b0 + vlb, idx = 12 * vbody + row;
+  double Dr[12];
+#pragma unroll
+  for (int c = 0; c < 12; ++c) Dr[c] = mine ? a.Dinv[144 * vbody + 12 * row + c] : 0.0;
+  double x_r = 0.0, r_r = 0.0, z_r = 0.0, pold_r = 0.0, q_r = 0.0, pv_r = 0.0;
+  // thread 0: the scene's carried scalars
+  int conv_r = 0;
+  double bb_r = 0.0, rz_r = 1.0;
+
+  // ---- init ----
+  {
+    double c0 = 0.0, c1 = 0.0;
+    if (mine) {
+      const bool on = a.sc_on[sc] != 0;
+      const double bv = on ? a.b[idx] : 0.0;
+      double zv = 0.0;
+      if (on) {
+#pragma unroll
+        for (int c = 0; c < 12; ++c) zv += Dr[c] * a.b[12 * vbody + c];
+      }
+      r_r = bv;
+      z_r = zv;
+      a.z[idx] = zv;
+      a.pbuf[idx] = 0.0;
+      a.pbuf[12 * a.nb + idx] = 0.0;
+      c0 = bv * bv;
+      c1 = bv * zv;
+    }
+    if (vthr) {
+      c0 = body_sum16(c0);
+      c1 = body_sum16(c1);
+    }
+    group_partial(c0, c1, s_w, a.gpB, g);
+  }
+  if (tid == 0) {
+    a.n_active[0] = 0;
+    a.n_active[1] = 0;
+    a.n_active[2] = 0;
+  }
+  grid.sync();
+  int k = 0;
+  for (;; ++k) {
+    const int par = k & 1;
+    const double* p_old = a.pbuf + (par ^ 1) * 12 * a.nb;
+    double* p_new = a.pbuf + par * 12 * a.nb;
+    if (tid == 0) a.n_active[(k + 1) % 3] = 0;
+    // ---- A_k ----
+    if (warp < 2) {
+      double v = warp_scene_sum(a.gpB, warp, a.sc_gbeg[sc], a.sc_gend[sc]);
+      if (lane == 0) s_sum[warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const double rr = s_sum[0], rz = s_sum[1];
+      int* conv_cur = a.sc_conv + par * a.ns;
+      if (k > 0 && conv_r) {
+        if (owner) conv_cur[sc] = 1;
+        s_flag = 1;
+      } else {
+        bool conv;
+        if (k == 0) {
+          conv = !a.sc_on[sc] || rr == 0.0;
+          if (owner) a.sc_bb[sc] = rr;
+          bb_r = rr;
+        } else {
+          conv = !(rr > a.tol2 * bb_r);
+        }
+        s_val = k == 0 ? 0.0 : rz / rz_r;
+        s_flag = conv || k == a.maxit;
+        conv_r = conv ? 1 : 0;
+        rz_r = rz;
+        if (owner) {
+          a.sc_rz[par * a.ns + sc] = rz;
+          conv_cur[sc] = conv ? 1 : 0;
+          if (conv) {
+            a.sc_iters[sc] = k;
+          } else if (k == a.maxit) {
+            a.sc_iters[sc] = k;
+            a.out[0] = ABD_ERR_PCG_NOCONV;
+          } else {
+            atomicAdd(&a.n_active[k % 3], 1);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const bool act = !s_flag;
+    const double beta = act ? s_val : 0.0;
+    double acc = 0.0;
+    if (act && pact) {
+      const unsigned half = 0xffffu << (threadIdx.x & 16);
+#pragma unroll
+      for (int jj = 0; jj < PCG1_NC; ++jj) {
+        const int j = part + NPART * jj;
+        if (j < pn) {
+          const int cb = rc[jj];
+          if (prow < 12) s_v[hg][prow] = dir(a.z[12 * cb + prow], beta, p_old[12 * cb + prow]);
+          __syncwarp(half);
+          if (prow < 12) {
+            const double2* v = reinterpret_cast<const double2*>(s_v[hg]);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+              double2 vv = v[c];
+              acc += hr[jj][2 * c] * vv.x;
+              acc += hr[jj][2 * c + 1] * vv.y;
+            }
+          }
+          __syncwarp(half);
+        }
+      }
+      for (int j = part + NPART * PCG1_NC; j < pn; j += NPART) {
+        const int cb = a.rcol[pbase + j];
+        if (prow < 12) s_v[hg][prow] = dir(a.z[12 * cb + prow], beta, p_old[12 * cb + prow]);
+        __syncwarp(half);
+        if (prow < 12) {
+          const double2* H = reinterpret_cast<const double2*>(a.Hrow + (size_t)(pbase + j) * 144 + 12 * prow);
+          const double2* v = reinterpret_cast<const double2*>(s_v[hg]);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            double2 h = H[c], vv = v[c];
+            acc += h.x * vv.x;
+            acc += h.y * vv.y;
+          }
+        }
+        __syncwarp(half);
+      }
+    }
+    s_part[threadIdx.x] = acc;
+    __syncthreads();
+    if (act) {
+      double c0 = 0.0;
+      if (mine) {
+        const double* sp = s_part + vlb * BODY_SLOTS + row;
+        double qv = sp[0];
+#pragma unroll
+        for (int pp = 1; pp < NPART; ++pp) qv += sp[16 * pp];
+        const double pv = dir(z_r, beta, pold_r);
+        p_new[idx] = pv;
+        pv_r = pv;
+        q_r = qv;
+        c0 = pv * qv;
+      }
+      if (vthr) c0 = body_sum16(c0);
+      group_partial(c0, 0.0, s_w, a.gpA, g);
+    }
+    __syncthreads();
+    if (k == a.maxit) break;
+    grid.sync();
+    if (ld_volatile(&a.n_active[k % 3]) == 0) break;
+    // ---- B_k (s_flag still holds whether the scene stopped in A_k: its CG ends there) ----
+    if (!s_flag) {
+      if (warp == 0) {
+        const double rz = lane == 0 ? rz_r : 0.0;
+        const double pq = warp_scene_sum(a.gpA, 0, a.sc_gbeg[sc], a.sc_gend[sc]);
+        if (lane == 0) s_val = rz / pq;
+      }
+      __syncthreads();
+      double c0 = 0.0, c1 = 0.0;
+      if (mine) {
+        const double alpha = s_val;
+        x_r += alpha * pv_r;
+        r_r -= alpha * q_r;
+      }
+      if (vthr) {
+        double zv = 0;
+#pragma unroll
+        for (int c = 0; c < 12; ++c) zv += Dr[c] * __shfl_sync(0xffffffffu, r_r, (lane & 16) + c);
+        if (mine) {
+          z_r = zv;
+          a.z[idx] = zv;
+          pold_r = pv_r;
+          c0 = r_r * r_r;
+          c1 = r_r * zv;
+        }
+        c0 = body_sum16(c0);
+        c1 = body_sum16(c1);
+      }
+      group_partial(c0, c1, s_w, a.gpB, g);
+    }
+    __syncthreads();
+    grid.sync();
+  }
+  if (mine) {
+    a.x[idx] = x_r;
+    a.dq[idx] = -x_r;
   }
   if (tid == 0) a.out[1] = k;
 }
@@ -1613,15 +1853,19 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
                                                                                         S.upidx.p, B.has.p, B.ovr.p,
                                                                                         B.D.p, B.Hrow.p, B.rcol.p,
                                                                                         B.rn.p, B.status.p + 2));
-  static int max_blocks = 0;
+  static int max_blocks = 0, max_blocks1 = 0;
   if (!max_blocks) {
-    int dev, sms, per;
+    int dev, sms, per, per1;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg, PCG_NT, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_pcg1, PCG_NT, 0));
     max_blocks = sms * (per > 0 ? per : 1);
+    max_blocks1 = sms * per1;
   }
-  int grid = B.ngrp < max_blocks ? B.ngrp : max_blocks;
+  // one group per CTA when the groups fit one cooperative wave, else groups in loop steps
+  const bool one = B.ngrp <= max_blocks1;
+  int grid = one ? B.ngrp : (B.ngrp < max_blocks ? B.ngrp : max_blocks);
   if (grid < 1) grid = 1;
   PcgArgs a;
   a.nb = nb;
@@ -1656,7 +1900,8 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   a.maxit = max_iter < 0 ? 0 : max_iter;
   a.out = B.status.p;
   void* args[] = {&a};
-  KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel((void*)k_pcg, dim3(grid), dim3(PCG_NT), args, 0, s)));
+  KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel(one ? (void*)k_pcg1 : (void*)k_pcg, dim3(grid), dim3(PCG_NT), args,
+                                                     0, s)));
   CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
   if (scene_iters) CK(cudaMemcpyAsync(scene_iters, B.sc_iters.p, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
