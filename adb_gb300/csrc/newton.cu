@@ -536,14 +536,34 @@ __global__ void __launch_bounds__(256) k_ov_reduce(int nov, const int* pt_seg, c
   int p0 = pt_seg[u], p1 = pt_seg[u + 1], e0 = ee_seg[u], e1 = ee_seg[u + 1];
   if (threadIdx.x == 0) has[u] = (p1 > p0) || (e1 > e0);
   if (p1 == p0 && e1 == e0) return;  // no pairs: the record is never read (has[u] = 0)
-  for (int c = w; c < CONTRIB; c += 8) {
+  // one thread per record entry, summing the overlap's pairs in order (each thread streams
+  // its own component row; no FP64 shuffle tree, which costs more than the sums on GB300)
+  (void)lane;
+  (void)w;
+  for (int c = threadIdx.x; c < CONTRIB; c += blockDim.x) {
     double s = 0.0;
-    for (int p = p0 + lane; p < p1; p += 32) s += ptC[(size_t)c * npt + p];
-    for (int p = e0 + lane; p < e1; p += 32) s += eeC[(size_t)c * nee + p];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const double* pr = ptC + (size_t)c * npt;
+    const double* er = eeC + (size_t)c * nee;
+    int p = p0;
+    for (; p + 3 < p1; p += 4) {
+      const double a0 = pr[p], a1 = pr[p + 1], a2 = pr[p + 2], a3 = pr[p + 3];
+      s += a0;
+      s += a1;
+      s += a2;
+      s += a3;
+    }
+    for (; p < p1; ++p) s += pr[p];
+    int e = e0;
+    for (; e + 3 < e1; e += 4) {
+      const double a0 = er[e], a1 = er[e + 1], a2 = er[e + 2], a3 = er[e + 3];
+      s += a0;
+      s += a1;
+      s += a2;
+      s += a3;
+    }
+    for (; e < e1; ++e) s += er[e];
     // the off-diagonal block takes the damping scale (1 + beta), like every matrix entry
-    if (lane == 0) ovr[(size_t)u * CONTRIB + c] = (c >= 288 && c < 432) ? s * off_scale : s;
+    ovr[(size_t)u * CONTRIB + c] = (c >= 288 && c < 432) ? s * off_scale : s;
   }
 }
 
@@ -555,7 +575,7 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
                                                      double* grad) {
   int b = blockIdx.x;
   int t = threadIdx.x;
-  if (t >= 156) return;
+  const bool ent = t < 156;  // threads 156..159 only help with the vertex-ground pairs
   bool is_h = t < 144;
   int i = is_h ? t / 12 : t - 144;
   int j = is_h ? t % 12 : 0;
@@ -567,6 +587,7 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
   if (m < 0.0 || !scene_on(g, b)) {
     // static body: identity block, zero gradient (mutils.cpp:55-56, 70); bodies of scenes
     // that are not iterating get the same (their step is zero)
+    if (!ent) return;
     if (is_h) {
       double v = (i == j) ? 1.0 : 0.0;
       // damping_sparse scales every body's block (mutils.cpp:106-115)
@@ -586,7 +607,7 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
   }
   double mi = (i < 3) ? m : g.Ic[b];
   double kap = 4.0 * P.ortho_kappa;
-  if (!(P.terms & TERM_INERTIA)) {
+  if (!ent || !(P.terms & TERM_INERTIA)) {
     // no inertia / orthogonality terms (adjoint of the friction terms alone)
   } else if (is_h) {
     val = (i == j) ? mi : 0.0;
@@ -618,40 +639,71 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
     val = dt * dt * og + mi * (q[i] - qt);
   }
   const bool vg_bar = (P.terms & TERM_BARRIER) != 0, vg_fr = (P.terms & TERM_FRICTION) && P.vg_fric;
-  // vertex-ground terms (barrier.cpp:31-69, friction with basis (e_x, e_z))
+  // vertex-ground terms (barrier.cpp:31-69, friction with basis (e_x, e_z)). The scalars
+  // of each pair (barrier derivatives, friction factors) are computed once, by one thread
+  // per pair, into shared memory; then every entry thread adds the pairs in order.
+  constexpr int VGC = 160;
+  __shared__ double s_n11[VGC], s_f1[VGC], s_g0[VGC], s_g2[VGC], s_M[VGC][4], s_xt[VGC][3];
+  __shared__ int s_on[VGC];
   BarrierP bp{P.dhat, P.kappa};
-  for (int kk = vg_seg[b]; kk < vg_seg[b + 1]; ++kk) {
-    int v = g.v_off[b] + vg[2 * kk + 1];
-    double py = g.X[g.nv + v];
-    double _d = py + P.ground_offset;
-    double dd = _d * _d;
-    if (!(dd < P.dhat)) {
-      if (t == 0) vg_lam[kk] = 0.0;
-      continue;
+  const int kb = vg_seg[b], ke = vg_seg[b + 1];
+  for (int c0 = kb; c0 < ke; c0 += VGC) {
+    const int cn = ke - c0 < VGC ? ke - c0 : VGC;
+    __syncthreads();
+    if (t < cn) {
+      const int kk = c0 + t;
+      int v = g.v_off[b] + vg[2 * kk + 1];
+      double py = g.X[g.nv + v];
+      double _d = py + P.ground_offset;
+      double dd = _d * _d;
+      const bool on = dd < P.dhat;
+      s_on[t] = on;
+      if (!on) {
+        vg_lam[kk] = 0.0;
+      } else {
+        double b1 = barrier_b1(dd, bp), b2 = barrier_b2(dd, bp);
+        double lamv = -b1 * 2 * _d;
+        vg_lam[kk] = lamv;
+        double uk[2] = {g.X[v] - g.X0[v], g.X[2 * g.nv + v] - g.X0[2 * g.nv + v]};
+        double gs = 0.0, M[2][2] = {{0, 0}, {0, 0}};
+        if (vg_fr) friction_2x2(uk, lamv, FrictionP{P.mu, P.epsv, P.max_uk}, gs, M);
+        // the reference drops b' d'' = 2 b' from the ground Hessian (barrier.cpp:62-69);
+        // the exact Hessian (adjoint systems) keeps it
+        s_n11[t] = vg_bar ? b2 * (2 * _d) * (2 * _d) + (P.exact ? 2 * b1 : 0.0) : 0.0;
+        s_f1[t] = vg_bar ? b1 * 2 * _d : 0.0;
+        s_g0[t] = gs * uk[0];
+        s_g2[t] = gs * uk[1];
+        s_M[t][0] = M[0][0];
+        s_M[t][1] = M[0][1];
+        s_M[t][2] = M[1][0];
+        s_M[t][3] = M[1][1];
+        s_xt[t][0] = g.rest[3 * v];
+        s_xt[t][1] = g.rest[3 * v + 1];
+        s_xt[t][2] = g.rest[3 * v + 2];
+      }
     }
-    double b1 = barrier_b1(dd, bp), b2 = barrier_b2(dd, bp);
-    double lamv = -b1 * 2 * _d;
-    if (t == 0) vg_lam[kk] = lamv;
-    double xt[4] = {1.0, g.rest[3 * v], g.rest[3 * v + 1], g.rest[3 * v + 2]};
-    double uk[2] = {g.X[v] - g.X0[v], g.X[2 * g.nv + v] - g.X0[2 * g.nv + v]};
-    double gs = 0.0, M[2][2] = {{0, 0}, {0, 0}};
-    if (vg_fr) friction_2x2(uk, lamv, FrictionP{P.mu, P.epsv, P.max_uk}, gs, M);
-    if (is_h) {
-      double N = 0.0;
-      // the reference drops b' d'' = 2 b' from the ground Hessian (barrier.cpp:62-69); the
-      // exact Hessian (adjoint systems) keeps it
-      if (r == 1 && s == 1 && vg_bar) N = b2 * (2 * _d) * (2 * _d) + (P.exact ? 2 * b1 : 0.0);
-      int rr = (r == 0) ? 0 : (r == 2 ? 1 : -1), ss = (s == 0) ? 0 : (s == 2 ? 1 : -1);
-      if (rr >= 0 && ss >= 0) N += M[rr][ss];
-      val += xt[k] * xt[l] * N;
-    } else {
-      double F = 0.0;
-      if (r == 1 && vg_bar) F = b1 * 2 * _d;
-      if (r == 0) F += gs * uk[0];
-      if (r == 2) F += gs * uk[1];
-      val += xt[k] * F;
-    }
+    __syncthreads();
+    if (ent)
+      for (int q = 0; q < cn; ++q) {
+        if (!s_on[q]) continue;
+        const double xk = k == 0 ? 1.0 : s_xt[q][k - 1];
+        if (is_h) {
+          double N = 0.0;
+          if (r == 1 && s == 1) N = s_n11[q];
+          int rr = (r == 0) ? 0 : (r == 2 ? 1 : -1), ss = (s == 0) ? 0 : (s == 2 ? 1 : -1);
+          if (rr >= 0 && ss >= 0) N += s_M[q][2 * rr + ss];
+          const double xl = l == 0 ? 1.0 : s_xt[q][l - 1];
+          val += xk * xl * N;
+        } else {
+          double F = 0.0;
+          if (r == 1) F = s_f1[q];
+          if (r == 0) F += s_g0[q];
+          if (r == 2) F += s_g2[q];
+          val += xk * F;
+        }
+      }
   }
+  if (!ent) return;
   // contact partial sums of the overlaps this body takes part in
   for (int e = row_ptr[b]; e < row_ptr[b + 1]; ++e) {
     int u = upidx[e];
