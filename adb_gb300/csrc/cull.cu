@@ -170,29 +170,41 @@ __device__ __forceinline__ void put_fbox(float* dst, const box& b) {
   dst[0] = __double2float_rd(b.lo.x); dst[1] = __double2float_rd(b.lo.y); dst[2] = __double2float_rd(b.lo.z);
   dst[3] = __double2float_ru(b.hi.x); dst[4] = __double2float_ru(b.hi.y); dst[5] = __double2float_ru(b.hi.z);
 }
-__global__ void k_prim_boxes(Geo g, int traj, float* vb, float* eb, float* fb) {
+// Float boxes of the primitives (outward rounded). Vertices first, from their FP64
+// positions (at X, or the trajectory from Xq to X); edges and faces are then the float
+// unions of their vertices' boxes: rounding down (up) commutes with min (max), so
+// rd(min(a, b)) = min(rd a, rd b) and the result equals rounding the FP64 box, without
+// any FP64 min/max.
+__global__ void k_vert_boxes(Geo g, int traj, float* vb) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  int nv = g.nv;
-  if (t < nv) {
-    d3 p = ldX(g.X, nv, t);
-    box b = traj ? box2(p, ldX(g.Xq, nv, t)) : box{p, p};
-    put_fbox(vb + 6 * t, b);
-    return;
+  if (t >= g.nv) return;
+  d3 p = ldX(g.X, g.nv, t);
+  box b = traj ? box2(p, ldX(g.Xq, g.nv, t)) : box{p, p};
+  put_fbox(vb + 6 * t, b);
+}
+__device__ __forceinline__ void fbox_union(float* o, const float* a, const float* b) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    o[c] = fminf(o[c], fminf(a[c], b[c]));
+    o[c + 3] = fmaxf(o[c + 3], fmaxf(a[c + 3], b[c + 3]));
   }
-  t -= nv;
+}
+__global__ void k_prim_boxes(Geo g, const float* vb, float* eb, float* fb) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  float o[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
   if (t < g.ne) {
-    int a = g.ev[2 * t], c = g.ev[2 * t + 1];
-    d3 p0 = ldX(g.X, nv, a), p1 = ldX(g.X, nv, c);
-    box b = traj ? box4(p0, p1, ldX(g.Xq, nv, a), ldX(g.Xq, nv, c)) : box2(p0, p1);
-    put_fbox(eb + 6 * t, b);
+    fbox_union(o, vb + 6 * g.ev[2 * t], vb + 6 * g.ev[2 * t + 1]);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) eb[6 * t + c] = o[c];
     return;
   }
   t -= g.ne;
   if (t < g.nf) {
-    int a = g.fv[3 * t], c = g.fv[3 * t + 1], d = g.fv[3 * t + 2];
-    box b = box3(ldX(g.X, nv, a), ldX(g.X, nv, c), ldX(g.X, nv, d));
-    if (traj) b = merge(box3(ldX(g.Xq, nv, a), ldX(g.Xq, nv, c), ldX(g.Xq, nv, d)), b);
-    put_fbox(fb + 6 * t, b);
+    const float* v2 = vb + 6 * g.fv[3 * t + 2];
+    fbox_union(o, vb + 6 * g.fv[3 * t], vb + 6 * g.fv[3 * t + 1]);
+    fbox_union(o, v2, v2);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) fb[6 * t + c] = o[c];
   }
 }
 
@@ -1130,8 +1142,11 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
   cs.vbox.ensure(6 * (size_t)g.nv + 6);
   cs.ebox.ensure(6 * (size_t)g.ne + 6);
   cs.fbox.ensure(6 * (size_t)g.nf + 6);
-  long long nprim = (long long)g.nv + g.ne + g.nf;
-  KLAUNCH(K_PRIM_BOXES, s, k_prim_boxes<<<nblk(nprim, 256), 256, 0, s>>>(g, traj, cs.vbox.p, cs.ebox.p, cs.fbox.p));
+  if (g.nv > 0) KLAUNCH(K_PRIM_BOXES, s, k_vert_boxes<<<nblk(g.nv, 256), 256, 0, s>>>(g, traj, cs.vbox.p));
+  if (g.ne + g.nf > 0) {
+    KLAUNCH(K_PRIM_BOXES, s, k_prim_boxes<<<nblk((long long)g.ne + g.nf, 256), 256, 0, s>>>(g, cs.vbox.p, cs.ebox.p,
+                                                                                             cs.fbox.p));
+  }
   int nlst = 0;
   if (nov > 0) {
     cs.bin_cnt.ensure(6 * (size_t)nov + 6);

@@ -1594,27 +1594,27 @@ __device__ __forceinline__ int scene_lower_bound(const int* bscene, const int* t
 }
 
 // Per-scene list offsets and chunk counts (thread per scene, plus one for the ends).
-__global__ void k_scene_offsets(Geo g, EnergyArgs a, int* off, int* chunk_cnt) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s > a.ns) return;
+// First element of each scene in each list (one thread per list and scene bound; the
+// lists are ordered by scene), then each scene's chunk count.
+__global__ void k_scene_offsets(Geo g, EnergyArgs a, int* off) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= NSEG * (a.ns + 1)) return;
+  const int k = t / (a.ns + 1), s = t - k * (a.ns + 1);
   const int* lists[NSEG] = {a.pt, a.ee, a.vg, a.lpt_t, a.lee_t, a.lvg_t};
   const int stride[NSEG] = {4, 4, 2, 4, 4, 2};
   const int n[NSEG] = {a.npt, a.nee, a.nvg, a.lpt, a.lee, a.lvg};
-  long long total = 0;
+  off[t] = (s == a.ns) ? n[k] : scene_lower_bound(g.bscene, lists[k], stride[k], n[k], s);
+}
+__global__ void k_scene_chunks(Geo g, EnergyArgs a, const int* off, int* chunk_cnt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.ns) return;
+  long long total = a.with_bi ? g.sc_end[s] - g.sc_beg[s] : 0;
   for (int k = 0; k < NSEG; ++k) {
-    int lo = (s == a.ns) ? n[k] : scene_lower_bound(g.bscene, lists[k], stride[k], n[k], s);
-    off[k * (a.ns + 1) + s] = lo;
-    if (s < a.ns) {
-      if (k < SEG_LPT && !a.with_bi) continue;
-      int hi = scene_lower_bound(g.bscene, lists[k], stride[k], n[k], s + 1);
-      total += hi - lo;
-    }
+    if (k < SEG_LPT && !a.with_bi) continue;
+    total += off[k * (a.ns + 1) + s + 1] - off[k * (a.ns + 1) + s];
   }
-  if (s < a.ns) {
-    if (a.with_bi) total += g.sc_end[s] - g.sc_beg[s];
-    long long c = (total + ECHUNK - 1) / ECHUNK;
-    chunk_cnt[s] = c > 0 ? (int)c : 1;
-  }
+  long long c = (total + ECHUNK - 1) / ECHUNK;
+  chunk_cnt[s] = c > 0 ? (int)c : 1;
 }
 
 __global__ void __launch_bounds__(256) k_energy(Geo g, Params P, EnergyArgs a) {
@@ -2017,7 +2017,8 @@ void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet&
   B.e_out.ensure(ns);
   a.off = B.e_off.p;
   a.chunk_off = B.e_chunk_off.p;
-  KLAUNCH(K_ENERGY, s, k_scene_offsets<<<nblk(ns + 1, 128), 128, 0, s>>>(g, a, B.e_off.p, B.e_chunk_cnt.p));
+  KLAUNCH(K_ENERGY, s, k_scene_offsets<<<nblk((long long)NSEG * (ns + 1), 128), 128, 0, s>>>(g, a, B.e_off.p));
+  KLAUNCH(K_ENERGY, s, k_scene_chunks<<<nblk(ns, 128), 128, 0, s>>>(g, a, B.e_off.p, B.e_chunk_cnt.p));
   scan_exclusive_int(B.e_chunk_cnt.p, B.e_chunk_off.p, ns, B.e_chunk_off.p + ns, s, B.e_scan_tmp);
   // chunk count bound: every scene has at least one chunk, plus one per ECHUNK terms
   long long terms = (long long)(with_bi ? g.nb + a.npt + a.nee + a.nvg : 0) + a.lpt + a.lee + a.lvg;
