@@ -723,44 +723,60 @@ __global__ void __launch_bounds__(160) k_body_system(Geo g, Params P, const int*
 }
 
 // Inverse of each SPD diagonal block via Cholesky (block-Jacobi preconditioner).
-__global__ void k_block_inverse(int nb, const double* D, double* Dinv, int* status) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  double L[12][12];
-  for (int i = 0; i < 12; ++i)
-    for (int j = 0; j < 12; ++j) L[i][j] = 0.5 * (D[144 * b + 12 * i + j] + D[144 * b + 12 * j + i]);
+// Inverse of each SPD diagonal block via Cholesky (block-Jacobi preconditioner), one warp
+// per block: lane i holds row i; the factor and its inverse pass through shared memory
+// between the column steps. The operations and their order are those of a serial
+// Cholesky and forward substitution.
+constexpr int BINV_W = 4;  // warps (blocks) per CTA
+__global__ void __launch_bounds__(32 * BINV_W) k_block_inverse(int nb, const double* D, double* Dinv, int* status) {
+  __shared__ double sL[BINV_W][12][12], sLi[BINV_W][12][12];
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * BINV_W + wi;
+  if (b >= nb) return;  // whole warps leave together
+  double(&L)[12][12] = sL[wi];
+  double(&Li)[12][12] = sLi[wi];
+  const bool rowl = lane < 12;
+  if (rowl)
+    for (int j = 0; j < 12; ++j) L[lane][j] = 0.5 * (D[144 * b + 12 * lane + j] + D[144 * b + 12 * j + lane]);
+  __syncwarp();
   for (int j = 0; j < 12; ++j) {
-    double s = L[j][j];
-    for (int k = 0; k < j; ++k) s -= L[j][k] * L[j][k];
-    if (!(s > 0)) {
-      atomicExch(status, (int)ABD_ERR_NOT_SPD);
-      s = 1e-300;
+    // diagonal entry by lane j, then the column below it by lanes i > j
+    if (lane == j) {
+      double s = L[j][j];
+      for (int k = 0; k < j; ++k) s -= L[j][k] * L[j][k];
+      if (!(s > 0)) {
+        atomicExch(status, (int)ABD_ERR_NOT_SPD);
+        s = 1e-300;
+      }
+      L[j][j] = sqrt(s);
     }
-    double l = sqrt(s);
-    L[j][j] = l;
-    for (int i = j + 1; i < 12; ++i) {
-      double t = L[i][j];
-      for (int k = 0; k < j; ++k) t -= L[i][k] * L[j][k];
-      L[i][j] = t / l;
+    __syncwarp();
+    if (rowl && lane > j) {
+      double t = L[lane][j];
+      for (int k = 0; k < j; ++k) t -= L[lane][k] * L[j][k];
+      L[lane][j] = t / L[j][j];
     }
+    __syncwarp();
   }
-  // inverse of L (lower), then Dinv = L^-T L^-1
-  double Li[12][12];
-  for (int i = 0; i < 12; ++i)
-    for (int j = 0; j < 12; ++j) Li[i][j] = 0.0;
-  for (int c = 0; c < 12; ++c) {
+  // column c of L^-1 by lane c (forward substitution)
+  if (rowl) {
+    const int c = lane;
     for (int i = 0; i < 12; ++i) {
       double t = (i == c) ? 1.0 : 0.0;
       for (int k = 0; k < i; ++k) t -= L[i][k] * Li[k][c];
-      Li[i][c] = t / L[i][i];
+      Li[i][c] = (i < c) ? 0.0 : t / L[i][i];
     }
   }
-  for (int i = 0; i < 12; ++i)
+  __syncwarp();
+  // Dinv = L^-T L^-1, row i by lane i
+  if (rowl) {
+    const int i = lane;
     for (int j = 0; j < 12; ++j) {
       double s = 0;
       for (int k = (i > j ? i : j); k < 12; ++k) s += Li[k][i] * Li[k][j];
       Dinv[144 * b + 12 * i + j] = s;
     }
+  }
 }
 
 // ---------------------------------------------------------------------------------
@@ -1880,7 +1896,8 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   B.status.ensure(4);
   if (!B.h_int) CK(cudaMallocHost(&B.h_int, 16 * sizeof(int)));
   CK(cudaMemsetAsync(B.status.p, 0, 4 * sizeof(int), s));
-  KLAUNCH(K_BLOCK_INVERSE, s, k_block_inverse<<<nblk(nb, 64), 64, 0, s>>>(nb, B.D.p, B.Dinv.p, B.status.p));
+  KLAUNCH(K_BLOCK_INVERSE, s, k_block_inverse<<<nblk(nb, BINV_W), 32 * BINV_W, 0, s>>>(nb, B.D.p, B.Dinv.p,
+                                                                                        B.status.p));
   B.x.ensure(12 * (size_t)nb);
   B.r.ensure(12 * (size_t)nb);
   B.z.ensure(12 * (size_t)nb);
