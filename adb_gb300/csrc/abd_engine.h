@@ -64,6 +64,7 @@ struct Geo {
                                         // the others get no pairs and identity blocks
   const double *q, *dq, *q0, *dqdt;     // nb * 12
   double *X, *Xq, *X0;                  // 3 * nv, structure of arrays (x | y | z)
+  double* qa;                           // nb * 12 scratch: the trial state q + alpha dq
 };
 
 __host__ __device__ inline bool scene_on(const Geo& g, int body) {

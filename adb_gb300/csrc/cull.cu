@@ -31,15 +31,22 @@ __device__ __forceinline__ d3 ldX(const double* X, int nv, int v) { return mk(X[
 // ---------------------------------------------------------------------------------
 // 1. projection: which 0 -> X0 at q0; 1 -> X and Xq at q; 2 -> X at q + alpha dq;
 //    3 -> Xq at q only
+// The trial state q + alpha dq of every body (alpha per scene when given), once per body
+// rather than once per vertex.
+__global__ void k_trial_state(Geo g, double alpha) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 12 * g.nb) return;
+  const int b = i / 12;
+  const double a = g.alpha_s ? g.alpha_s[g.bscene[b]] : alpha;
+  g.qa[i] = XA(g.q[i], XM(g.dq[i], a));
+}
+
 __global__ void k_project(Geo g, int which, double alpha) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= g.nv) return;
   int b = g.vbody[v];
-  double qq[12];
-  const double* q = (which == 0) ? g.q0 + 12 * b : g.q + 12 * b;
-  if (which == 2 && g.alpha_s) alpha = g.alpha_s[g.bscene[b]];
-#pragma unroll
-  for (int i = 0; i < 12; ++i) qq[i] = (which == 2) ? XA(q[i], XM(g.dq[12 * b + i], alpha)) : q[i];
+  (void)alpha;
+  const double* qq = (which == 0) ? g.q0 + 12 * b : ((which == 2) ? g.qa + 12 * b : g.q + 12 * b);
   d3 x = project(qq, g.rest[3 * v], g.rest[3 * v + 1], g.rest[3 * v + 2]);
   double* dst = (which == 0) ? g.X0 : ((which == 3) ? g.Xq : g.X);
   dst[v] = x.x;
@@ -1085,6 +1092,7 @@ double key_to_double(unsigned long long k) {
 }  // namespace
 
 void launch_project(const Geo& g, int which, double alpha, cudaStream_t s) {
+  if (which == 2 && g.nb > 0) KLAUNCH(K_PROJECT, s, k_trial_state<<<nblk(12ll * g.nb, 256), 256, 0, s>>>(g, alpha));
   if (g.nv == 0) return;
   KLAUNCH(K_PROJECT, s, k_project<<<nblk(g.nv, 256), 256, 0, s>>>(g, which, alpha));
   prof_work(K_PROJECT, g.nv, 48.0 * g.nv);  // rest read + world write per vertex

@@ -83,7 +83,7 @@ struct Engine {
   int max_prims = 0;                             // most vertices + edges + faces of one body
   cudaStream_t s = nullptr;
   DBuf<int> v_off, e_off, f_off, vbody, ev, fv, scene_beg, scene_end;
-  DBuf<double> rest, mass, Ic, rest_box, q, q0, dqdt, dq, X, Xq, X0, lastdq;
+  DBuf<double> rest, mass, Ic, rest_box, q, q0, dqdt, dq, X, Xq, X0, lastdq, qa;
   PairSet sets[3];
   int cur = 0;
   CullScratch cs;
@@ -116,7 +116,7 @@ struct Engine {
     g.ns = ns; g.bscene = bscene.p; g.sc_beg = sc_beg.p; g.sc_end = sc_end.p; g.alpha_s = nullptr;
     g.sc_act = nullptr;
     g.q = q.p; g.dq = dq.p; g.q0 = q0.p; g.dqdt = dqdt.p;
-    g.X = X.p; g.Xq = Xq.p; g.X0 = X0.p;
+    g.X = X.p; g.Xq = Xq.p; g.X0 = X0.p; g.qa = qa.p;
     return g;
   }
 
@@ -125,7 +125,7 @@ struct Engine {
                        &bscene, &sc_beg, &sc_end, &sc_on, &sc_iter, &sc_search};
     for (auto* b : ib) b->release();
     DBuf<double>* db[] = {&rest, &mass, &Ic, &rest_box, &q, &q0, &dqdt, &dq, &X, &Xq, &X0, &sc_alpha, &sc_factor,
-                          &lastdq};
+                          &lastdq, &qa};
     for (auto* b : db) b->release();
     for (auto& S : sets) {
       S.row_ptr.release(); S.col.release(); S.upidx.release(); S.ovI.release(); S.ovJ.release();
@@ -320,6 +320,7 @@ struct Engine {
     has_lastdq.assign(ns, 0);
     X.ensure(3 * (size_t)nv + 3);
     Xq.ensure(3 * (size_t)nv + 3);
+    qa.ensure(12 * (size_t)nb + 12);
     X0.ensure(3 * (size_t)nv + 3);
     CK(cudaStreamSynchronize(s));
   }
