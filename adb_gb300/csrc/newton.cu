@@ -1261,6 +1261,7 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg1(PcgArgs a) {
   __shared__ __align__(16) double s_v[PCG_NT / 16][12];
   __shared__ double s_sum[2];
   __shared__ double s_val;
+  __shared__ double s_beta, s_rzp;  // beta from warp 1's r.z sum; the previous r.z
   __shared__ int s_flag;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1336,7 +1337,11 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg1(PcgArgs a) {
     // ---- A_k ----
     if (warp < 2) {
       double v = warp_scene_sum(a.gpB, warp, a.sc_gbeg[sc], a.sc_gend[sc]);
-      if (lane == 0) s_sum[warp] = v;
+      if (lane == 0) {
+        s_sum[warp] = v;
+        // beta = r.z / previous r.z, divided here beside warp 0's sum instead of after it
+        if (warp == 1 && k > 0) s_beta = v / s_rzp;
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1354,10 +1359,11 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg1(PcgArgs a) {
         } else {
           conv = !(rr > a.tol2 * bb_r);
         }
-        s_val = k == 0 ? 0.0 : rz / rz_r;
+        s_val = k == 0 ? 0.0 : s_beta;
         s_flag = conv || k == a.maxit;
         conv_r = conv ? 1 : 0;
         rz_r = rz;
+        s_rzp = rz;
         if (owner) {
           a.sc_rz[par * a.ns + sc] = rz;
           conv_cur[sc] = conv ? 1 : 0;
@@ -1378,12 +1384,19 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg1(PcgArgs a) {
     double acc = 0.0;
     if (act && pact) {
       const unsigned half = 0xffffu << (threadIdx.x & 16);
+      // the neighbour entries of both register blocks are loaded before either is used
+      double zn[PCG1_NC], pn_[PCG1_NC];
+#pragma unroll
+      for (int jj = 0; jj < PCG1_NC; ++jj) {
+        const bool ld = part + NPART * jj < pn && prow < 12;
+        zn[jj] = ld ? a.z[12 * rc[jj] + prow] : 0.0;
+        pn_[jj] = ld ? p_old[12 * rc[jj] + prow] : 0.0;
+      }
 #pragma unroll
       for (int jj = 0; jj < PCG1_NC; ++jj) {
         const int j = part + NPART * jj;
         if (j < pn) {
-          const int cb = rc[jj];
-          if (prow < 12) s_v[hg][prow] = dir(a.z[12 * cb + prow], beta, p_old[12 * cb + prow]);
+          if (prow < 12) s_v[hg][prow] = dir(zn[jj], beta, pn_[jj]);
           __syncwarp(half);
           if (prow < 12) {
             const double2* v = reinterpret_cast<const double2*>(s_v[hg]);
@@ -1435,14 +1448,14 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg1(PcgArgs a) {
     __syncthreads();
     if (k == a.maxit) break;
     grid.sync();
-    if (ld_volatile(&a.n_active[k % 3]) == 0) break;
+    // the count of scenes still iterating and the p.q partials are loaded together
+    const int nact = ld_volatile(&a.n_active[k % 3]);
+    double pq = 0.0;
+    if (!s_flag && warp == 0) pq = warp_scene_sum(a.gpA, 0, a.sc_gbeg[sc], a.sc_gend[sc]);
+    if (nact == 0) break;
     // ---- B_k (s_flag still holds whether the scene stopped in A_k: its CG ends there) ----
     if (!s_flag) {
-      if (warp == 0) {
-        const double rz = lane == 0 ? rz_r : 0.0;
-        const double pq = warp_scene_sum(a.gpA, 0, a.sc_gbeg[sc], a.sc_gend[sc]);
-        if (lane == 0) s_val = rz / pq;
-      }
+      if (threadIdx.x == 0) s_val = rz_r / pq;
       __syncthreads();
       double c0 = 0.0, c1 = 0.0;
       if (mine) {

@@ -1,6 +1,8 @@
 // Deterministic device exclusive scans (int and int64) used by the ordered compactions
 // of the culling stages: block-local scans, a recursive scan of the block totals, and
-// an add pass. The result does not depend on scheduling.
+// an add pass. The result does not depend on scheduling. The grand total is written by
+// the tile scan (one tile) or by the add pass (several), not by a launch of its own:
+// a scan of up to 2048 entries is one launch.
 #include "abd_engine.h"
 
 namespace abd {
@@ -39,7 +41,7 @@ __device__ T block_excl_scan(T v, T* sh, T& total) {
 }
 
 template <typename T>
-__global__ void k_scan_tiles(const T* in, T* out, int n, T* tile_sums) {
+__global__ void k_scan_tiles(const T* in, T* out, int n, T* tile_sums, T* grand) {
   __shared__ T sh[32];
   int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
   T v[SCAN_ITEMS];
@@ -58,36 +60,39 @@ __global__ void k_scan_tiles(const T* in, T* out, int n, T* tile_sums) {
     if (i < n) out[i] = pre;
     pre += v[k];
   }
-  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+  if (threadIdx.x == 0) {
+    tile_sums[blockIdx.x] = total;
+    if (grand && gridDim.x == 1) *grand = total;
+  }
 }
 
 template <typename T>
-__global__ void k_scan_add(T* out, int n, const T* tile_off) {
+__global__ void k_scan_add(T* out, int n, const T* tile_off, const T* in, T* grand) {
   int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
   T add = tile_off[blockIdx.x];
 #pragma unroll
   for (int k = 0; k < SCAN_ITEMS; ++k) {
     int i = base + k;
-    if (i < n) out[i] += add;
+    if (i < n) {
+      const T v = out[i] + add;
+      out[i] = v;
+      if (grand && i == n - 1) *grand = v + in[i];
+    }
   }
 }
 
+// Exclusive scan of in[0, n) into out; *grand (if not null) receives the total.
 template <typename T>
-__global__ void k_total(const T* in, const T* out, int n, T* total) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *total = (n > 0) ? out[n - 1] + in[n - 1] : T(0);
-}
-
-template <typename T>
-void scan_rec(const T* in, T* out, int n, cudaStream_t s, T* tmp, size_t tmp_cap) {
+void scan_rec(const T* in, T* out, int n, cudaStream_t s, T* tmp, size_t tmp_cap, T* grand) {
   if (n <= 0) return;
   int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
   T* sums = tmp;
   T* sums_off = tmp + tiles;
   if ((size_t)(2 * tiles) > tmp_cap) throw CudaError{cudaErrorMemoryAllocation, "scan scratch"};
-  KLAUNCH(K_SCAN, s, (k_scan_tiles<T><<<tiles, SCAN_T, 0, s>>>(in, out, n, sums)));
+  KLAUNCH(K_SCAN, s, (k_scan_tiles<T><<<tiles, SCAN_T, 0, s>>>(in, out, n, sums, grand)));
   if (tiles > 1) {
-    scan_rec<T>(sums, sums_off, tiles, s, tmp + 2 * tiles, tmp_cap - 2 * tiles);
-    KLAUNCH(K_SCAN, s, (k_scan_add<T><<<tiles, SCAN_T, 0, s>>>(out, n, sums_off)));
+    scan_rec<T>(sums, sums_off, tiles, s, tmp + 2 * tiles, tmp_cap - 2 * tiles, nullptr);
+    KLAUNCH(K_SCAN, s, (k_scan_add<T><<<tiles, SCAN_T, 0, s>>>(out, n, sums_off, in, grand)));
   }
 }
 
@@ -105,21 +110,15 @@ size_t scan_scratch(int n) {
 
 void scan_exclusive_int(const int* in, int* out, int n, int* d_total, cudaStream_t s, DBuf<int>& tmp) {
   tmp.ensure(scan_scratch<int>(n) + 8);
-  scan_rec<int>(in, out, n, s, tmp.p, tmp.cap);
-  if (d_total) {
-    if (n > 0) KLAUNCH(K_SCAN, s, (k_total<int><<<1, 32, 0, s>>>(in, out, n, d_total)));
-    else CK(cudaMemsetAsync(d_total, 0, sizeof(int), s));
-  }
+  scan_rec<int>(in, out, n, s, tmp.p, tmp.cap, d_total);
+  if (d_total && n <= 0) CK(cudaMemsetAsync(d_total, 0, sizeof(int), s));
 }
 
 void scan_exclusive_ll(const long long* in, long long* out, int n, long long* d_total, cudaStream_t s,
                        DBuf<long long>& tmp) {
   tmp.ensure(scan_scratch<long long>(n) + 8);
-  scan_rec<long long>(in, out, n, s, tmp.p, tmp.cap);
-  if (d_total) {
-    if (n > 0) KLAUNCH(K_SCAN, s, (k_total<long long><<<1, 32, 0, s>>>(in, out, n, d_total)));
-    else CK(cudaMemsetAsync(d_total, 0, sizeof(long long), s));
-  }
+  scan_rec<long long>(in, out, n, s, tmp.p, tmp.cap, d_total);
+  if (d_total && n <= 0) CK(cudaMemsetAsync(d_total, 0, sizeof(long long), s));
 }
 
 }  // namespace abd
