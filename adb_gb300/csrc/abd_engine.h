@@ -111,6 +111,7 @@ struct CullScratch {
   DBuf<uint8_t> flags;
   DBuf<int> blk_a, blk_b, blk_a_off, blk_b_off;
   DBuf<int> vflag_cnt, vflag_off, sub_cnt, stage_off;
+  DBuf<int> vg_cnt;  // vertex-ground pairs per block of vertices
   DBuf<unsigned long long> stage_key;   // sorted accepted pairs per overlap (sub, i, j)
   DBuf<int8_t> stage_ty;
   DBuf<unsigned long long> toi_key;     // 2 per scene: pt/ee, ground
@@ -182,6 +183,8 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
 
 // Vertex-ground pairs (d = (y + ground_offset)^2 < P.dhat) into S.vg / S.vg_seg.
 void vg_pairs(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, cudaStream_t s);
+void vg_count(const Geo& g, const Params& P, CullScratch& cs, cudaStream_t s);
+void vg_write(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, int nvg, cudaStream_t s);
 // Ground times of impact of all vertices into the ground slots of the per-scene keys.
 void launch_vg_toi(const Geo& g, const Params& P, unsigned long long* toi_key, cudaStream_t s);
 

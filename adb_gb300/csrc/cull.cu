@@ -1124,12 +1124,15 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
   KLAUNCH(K_BODY_BOXES, s, k_body_boxes<<<nblk(nb, 128), 128, 0, s>>>(g, vtn, alpha, cs.bbox.p));
   KLAUNCH(K_OV_COUNT, s, k_ov_count<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, cs.cnt_all.p, cs.cnt_up.p));
   cs.tmp_int.ensure(64);
-  int* d_tot = cs.tmp_int.p;  // [0] nnz, [1] nov
+  int* d_tot = cs.tmp_int.p;  // [0] nnz, [1] nov, [2] list entries, [3] PT, [4] EE, [5] VG, [6] staged
   scan_exclusive_int(cs.cnt_all.p, S.row_ptr.p, nb, d_tot, s, cs.vflag_cnt);
   scan_exclusive_int(cs.cnt_up.p, cs.up_ptr.p, nb, d_tot + 1, s, cs.vflag_cnt);
-  CK(cudaMemcpyAsync(cs.h_small, d_tot, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  // the vertex-ground pairs need only the positions: counted now, read with the overlaps
+  if (!traj) vg_count(g, P, cs, s);
+  CK(cudaMemcpyAsync(cs.h_small, d_tot, 6 * sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   int nnz = cs.h_small[0], nov = cs.h_small[1];
+  const int nvg = traj ? 0 : cs.h_small[5];
   CK(cudaMemcpyAsync(S.row_ptr.p + nb, d_tot, sizeof(int), cudaMemcpyDeviceToDevice, s));
   S.nnz = nnz;
   S.nov = nov;
@@ -1171,9 +1174,14 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
                                                           cs.fbox.p, cs.bin_cnt.p, nullptr, nullptr));
     }
     scan_exclusive_int(cs.bin_cnt.p, cs.bin_off.p, 6 * nov, d_tot + 2, s, cs.vflag_cnt);
-    CK(cudaMemcpyAsync(cs.h_small + 2, d_tot + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    nlst = cs.h_small[2];
+    if (once) {
+      // the capacities sum to at most both bodies' primitive counts per overlap
+      nlst = (int)(2ll * nov * g.max_prims);
+    } else {
+      CK(cudaMemcpyAsync(cs.h_small + 2, d_tot + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      nlst = cs.h_small[2];
+    }
     cs.lst.ensure((size_t)nlst + 1);
     KLAUNCH(K_BIN, s, k_bin<<<nblk((long long)nw * 32, 256), 256, 0, s>>>(g, nov, once ? BIN_ONCE : BIN_WRITE, traj,
                                                         S.ovI.p, S.ovJ.p, cs.ovcull.p, cs.ovcull_f.p, cs.vbox.p,
@@ -1244,18 +1252,17 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
                                                                       cs.fbox.p, cs.sub_cnt.p, nullptr, cs.stage_key.p,
                                                                       cs.stage_ty.p, cs.stage_off.p, d_tot + 6,
                                                                       (int)cs.stage_key.cap, cs.order.p));
-      CK(cudaMemcpyAsync(cs.h_small + 6, d_tot + 6, sizeof(int), cudaMemcpyDeviceToHost, s));
+      // per-overlap pair counts and their offsets, read together with the staged total
+      KLAUNCH(K_NARROW_WRITE, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
+      scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
+      scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
+      CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       if ((size_t)cs.h_small[6] <= cs.stage_key.cap) break;
       // staging overflowed: grow to the reported total and classify again
       cs.stage_key.ensure((size_t)cs.h_small[6] + (cs.h_small[6] >> 2) + 1024);
       cs.stage_ty.ensure(cs.stage_key.cap);
     }
-    KLAUNCH(K_NARROW_WRITE, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
-    scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
-    scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
-    CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
     npt = cs.h_small[3];
     nee = cs.h_small[4];
     prof_work(K_NARROW_SCAN, nov, 24.0 * g.nv + 20.0 * ((double)npt + nee));
@@ -1276,35 +1283,50 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
   }
   S.npt = npt;
   S.nee = nee;
-  // 6. vertex-ground pairs
-  vg_pairs(g, P, cs, S, s);
+  // 6. vertex-ground pairs (counted before the overlaps were read)
+  vg_write(g, P, cs, S, nvg, s);
 }
 
-void vg_pairs(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, cudaStream_t s) {
-  const int nb = g.nb;
-  int nvg = 0;
-  S.vg_seg.ensure(nb + 2);
+// Vertex-ground pairs in two halves around the host's read of their count (d_tot[5]):
+// vg_count launches the per-block counts and their scan, vg_write the ordered write and
+// the per-body segments.
+void vg_count(const Geo& g, const Params& P, CullScratch& cs, cudaStream_t s) {
   cs.tmp_int.ensure(64);
   int* d_tot = cs.tmp_int.p;
-  if (!cs.h_small) {
-    CK(cudaMallocHost(&cs.h_small, 64 * sizeof(int)));
-    CK(cudaMallocHost(&cs.h_ll, 8 * sizeof(long long)));
-  }
   if (P.ground && g.nv) {
     int nbv = nblk(g.nv, 256);
     cs.vflag_off.ensure(nbv + 1);
-    cs.blk_a.ensure(nbv + 1);
-    KLAUNCH(K_VG, s, k_vg_count<<<nbv, 256, 0, s>>>(g, P, cs.blk_a.p));
-    scan_exclusive_int(cs.blk_a.p, cs.vflag_off.p, nbv, d_tot + 5, s, cs.vflag_cnt);
-    CK(cudaMemcpyAsync(cs.h_small + 5, d_tot + 5, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    nvg = cs.h_small[5];
+    cs.vg_cnt.ensure(nbv + 1);
+    KLAUNCH(K_VG, s, k_vg_count<<<nbv, 256, 0, s>>>(g, P, cs.vg_cnt.p));
+    scan_exclusive_int(cs.vg_cnt.p, cs.vflag_off.p, nbv, d_tot + 5, s, cs.vflag_cnt);
+  } else {
+    CK(cudaMemsetAsync(d_tot + 5, 0, sizeof(int), s));
+  }
+}
+
+void vg_write(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, int nvg, cudaStream_t s) {
+  const int nb = g.nb;
+  S.vg_seg.ensure(nb + 2);
+  if (P.ground && g.nv) {
     S.vg.ensure(2 * (size_t)nvg + 2);
-    KLAUNCH(K_VG, s, k_vg_write<<<nbv, 256, 0, s>>>(g, P, cs.vflag_off.p, S.vg.p));
+    KLAUNCH(K_VG, s, k_vg_write<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, cs.vflag_off.p, S.vg.p));
+  } else {
+    nvg = 0;
   }
   S.nvg = nvg;
   S.vg.ensure(2);
   KLAUNCH(K_VG, s, k_vg_seg<<<nblk(nb + 1, 256), 256, 0, s>>>(nb, nvg, S.vg.p, S.vg_seg.p));
+}
+
+void vg_pairs(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, cudaStream_t s) {
+  if (!cs.h_small) {
+    CK(cudaMallocHost(&cs.h_small, 64 * sizeof(int)));
+    CK(cudaMallocHost(&cs.h_ll, 8 * sizeof(long long)));
+  }
+  vg_count(g, P, cs, s);
+  CK(cudaMemcpyAsync(cs.h_small + 5, cs.tmp_int.p + 5, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  vg_write(g, P, cs, S, cs.h_small[5], s);
 }
 
 void launch_vg_toi(const Geo& g, const Params& P, unsigned long long* toi_key, cudaStream_t s) {

@@ -137,7 +137,7 @@ struct Engine {
     cs.order.release(); cs.order_cnt.release();
     cs.bin_cnt.release(); cs.bin_off.release(); cs.lst.release(); cs.cand_cnt.release(); cs.cand_off.release();
     cs.flags.release(); cs.blk_a.release(); cs.blk_b.release(); cs.blk_a_off.release(); cs.blk_b_off.release();
-    cs.vflag_cnt.release(); cs.vflag_off.release(); cs.sub_cnt.release(); cs.stage_off.release();
+    cs.vflag_cnt.release(); cs.vflag_off.release(); cs.sub_cnt.release(); cs.stage_off.release(); cs.vg_cnt.release();
     cs.stage_key.release(); cs.stage_ty.release(); cs.toi_key.release(); cs.tmp_int.release(); cs.tmp_ll.release();
     if (cs.h_small) cudaFreeHost(cs.h_small);
     if (cs.h_ll) cudaFreeHost(cs.h_ll);

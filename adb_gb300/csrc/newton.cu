@@ -532,14 +532,11 @@ __global__ void __launch_bounds__(256) k_ov_reduce(int nov, const int* pt_seg, c
                                                    double off_scale) {
   int u = blockIdx.x;
   if (u >= nov) return;
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int p0 = pt_seg[u], p1 = pt_seg[u + 1], e0 = ee_seg[u], e1 = ee_seg[u + 1];
   if (threadIdx.x == 0) has[u] = (p1 > p0) || (e1 > e0);
   if (p1 == p0 && e1 == e0) return;  // no pairs: the record is never read (has[u] = 0)
   // one thread per record entry, summing the overlap's pairs in order (each thread streams
   // its own component row; no FP64 shuffle tree, which costs more than the sums on GB300)
-  (void)lane;
-  (void)w;
   for (int c = threadIdx.x; c < CONTRIB; c += blockDim.x) {
     double s = 0.0;
     const double* pr = ptC + (size_t)c * npt;
