@@ -253,7 +253,7 @@ __global__ void k_bin_caps(Geo g, int nov, const int* ovI, const int* ovJ, int* 
   cap[t] = o[body + 1] - o[body];
 }
 
-__global__ void k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const int* ovJ, const double* ovcull,
+__global__ void __launch_bounds__(256, 3) k_bin(Geo g, int nov, int pass, int traj, const int* ovI, const int* ovJ, const double* ovcull,
                       const float* ovcull_f, const float* vb, const float* eb, const float* fb, int* cnt,
                       const int* off, int* lst) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
