@@ -325,11 +325,15 @@ __global__ void __launch_bounds__(256, 3) k_bin(Geo g, int nov, int pass, int tr
 constexpr int NT = 256;     // narrow-phase threads per CTA
 constexpr int TILE = 384;   // primitives of one list staged in shared memory (2 x 9 kB)
 constexpr int REC_CAP = 2048;  // accepted pairs of one overlap kept in shared memory for sorting
-constexpr int STEP = 64;    // box-phase candidates per thread between two exact phases
-constexpr int QCAP = NT * STEP;  // queue of float-box hits (64 kB)
+// Box-phase candidates per thread between two exact phases, and the queue of float-box
+// hits they fill: 64 (a 64 kB queue, two CTAs per SM) for the pair cull; 36 for the CCD,
+// whose smaller queue lets three CTAs share an SM (its time-of-impact tests gain more
+// from the extra CTAs than from the longer box phases).
+__host__ __device__ constexpr int narrow_step(int mode) { return mode == 2 ? 36 : 64; }
+__host__ __device__ constexpr int narrow_qcap(int mode) { return NT * narrow_step(mode); }
 // dynamic shared memory of k_narrow_scan<MODE>: boxes, queue, accepted pairs (MODE 0)
 __host__ __device__ constexpr size_t narrow_smem(int mode) {
-  return 2 * TILE * 6 * sizeof(float) + QCAP * sizeof(unsigned) +
+  return 2 * TILE * 6 * sizeof(float) + narrow_qcap(mode) * sizeof(unsigned) +
          (mode == 0 ? REC_CAP * (sizeof(unsigned long long) + 1) : 0);
 }
 
@@ -703,7 +707,7 @@ __global__ void k_order_place(int nov, const int* cnt, int* bc, int* order) {
 //  - exact phase: the whole CTA takes the queued candidates round-robin for the exact
 //    FP64 test (MODE 0: box, lower bounds, type and distance; MODE 2: time of impact).
 template <int MODE>
-__global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
+__global__ void __launch_bounds__(NT, MODE == 2 ? 3 : 2) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
                                                     int* cnt, const int* off, int* lst, const float* vb,
                                                     const float* eb, const float* fb, int* sub_cnt,
                                                     unsigned long long* toi_key, unsigned long long* stage_key,
@@ -714,7 +718,8 @@ __global__ void __launch_bounds__(NT, 2) k_narrow_scan(Geo g, Params P, float ds
   float* sA = reinterpret_cast<float*>(smem_dyn + (MODE == 0 ? REC_CAP * sizeof(unsigned long long) : 0));
   float* sB = sA + TILE * 6;
   unsigned int* sq = reinterpret_cast<unsigned int*>(sB + TILE * 6);
-  int8_t* recT = reinterpret_cast<int8_t*>(sq + QCAP);                         // REC_CAP (MODE 0)
+  constexpr int STEP = narrow_step(MODE);
+  int8_t* recT = reinterpret_cast<int8_t*>(sq + narrow_qcap(MODE));                         // REC_CAP (MODE 0)
   __shared__ int sq_n[2];
   __shared__ int rec_n, rec_base;
   const int u = order[blockIdx.x];
