@@ -1493,7 +1493,7 @@ __global__ void __launch_bounds__(PCG_NT) k_pcg1(PcgArgs a) {
 // scene's own start, each chunk is summed by one block in a fixed order, and the chunk
 // sums of a scene are added in chunk order. The total of a scene therefore does not
 // depend on where the scene sits in a batch.
-constexpr int ECHUNK = 1024;
+constexpr int ECHUNK = 512;
 enum { SEG_PT, SEG_EE, SEG_VG, SEG_LPT, SEG_LEE, SEG_LVG, NSEG };
 
 struct EnergyArgs {

@@ -81,11 +81,63 @@ __global__ void k_scan_add(T* out, int n, const T* tile_off, const T* in, T* gra
   }
 }
 
+// Scans of up to SCAN_ONE entries in one CTA (one launch instead of three): each thread
+// sums a contiguous run of ONE_ITEMS entries, the CTA scans the run sums, and each thread
+// writes its run from its offset.
+constexpr int ONE_T = 1024;
+constexpr int ONE_ITEMS = 16;
+constexpr int SCAN_ONE = ONE_T * ONE_ITEMS;
+template <typename T>
+__global__ void __launch_bounds__(ONE_T) k_scan_one(const T* in, T* out, int n, T* grand) {
+  __shared__ T sh[32];
+  const int base = threadIdx.x * ONE_ITEMS;
+  T v[ONE_ITEMS];
+  T loc = 0;
+#pragma unroll
+  for (int k = 0; k < ONE_ITEMS; ++k) {
+    const int i = base + k;
+    v[k] = (i < n) ? in[i] : T(0);
+    loc += v[k];
+  }
+  // CTA exclusive scan of the run sums (warp scans, then the warp totals)
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T x = loc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    T t = sh[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    sh[lane] = t;
+  }
+  __syncthreads();
+  T pre = (w > 0 ? sh[w - 1] : T(0)) + x - loc;
+#pragma unroll
+  for (int k = 0; k < ONE_ITEMS; ++k) {
+    const int i = base + k;
+    if (i < n) out[i] = pre;
+    pre += v[k];
+  }
+  if (grand && threadIdx.x == 0) *grand = sh[31];
+}
+
 // Exclusive scan of in[0, n) into out; *grand (if not null) receives the total.
 template <typename T>
 void scan_rec(const T* in, T* out, int n, cudaStream_t s, T* tmp, size_t tmp_cap, T* grand) {
   if (n <= 0) return;
   int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (tiles > 1 && n <= SCAN_ONE) {
+    KLAUNCH(K_SCAN, s, (k_scan_one<T><<<1, ONE_T, 0, s>>>(in, out, n, grand)));
+    return;
+  }
   T* sums = tmp;
   T* sums_off = tmp + tiles;
   if ((size_t)(2 * tiles) > tmp_cap) throw CudaError{cudaErrorMemoryAllocation, "scan scratch"};
