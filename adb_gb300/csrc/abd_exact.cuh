@@ -234,51 +234,6 @@ HD double ee_dist(d3 a0, d3 a1, d3 b0, d3 b1, int ty) {
 }
 
 // ---------------------------------------------------------------------------------
-// Cheap rejection before the exact classification. The point-triangle distance is at
-// least the distance from the point to the triangle's AABB and at least its distance
-// to the triangle's plane; the segment-segment distance is at least the AABB-to-AABB
-// distance and the line-line distance. When such a lower bound exceeds dhat by a
-// relative margin of 1e-6 -- far above the rounding of both the bound and the exact
-// distance formulas -- the exact path would reject the pair too, so it is skipped. The
-// bounds are only used on well-shaped geometry (no edge shorter than 1e-3 sqrt(dhat),
-// no sliver triangles, no near-parallel edge pairs), where the exact formulas' rounding
-// is bounded; everything else goes through the exact path.
-HD bool lb_reject_pt(d3 p, d3 t0, d3 t1, d3 t2, double dhat) {
-  const double lim = dhat * (1.0 + 1e-6);
-  d3 e1 = sub(t1, t0), e2 = sub(t2, t0), e3 = sub(t2, t1);
-  double l1 = sqn(e1), l2 = sqn(e2), l3 = sqn(e3);
-  double lmin = l1 < l2 ? l1 : l2;
-  lmin = lmin < l3 ? lmin : l3;
-  if (!(lmin >= 1e-6 * dhat)) return false;
-  d3 n = cross(e1, e2);
-  double nn = sqn(n);
-  if (!(nn >= 1e-6 * l1 * l2)) return false;
-  d3 lo = vmin(vmin(t0, t1), t2), hi = vmax(vmax(t0, t1), t2);
-  double bx = dmax(0.0, dmax(lo.x - p.x, p.x - hi.x));
-  double by = dmax(0.0, dmax(lo.y - p.y, p.y - hi.y));
-  double bz = dmax(0.0, dmax(lo.z - p.z, p.z - hi.z));
-  if (bx * bx + by * by + bz * bz >= lim) return true;
-  double s = dot(sub(p, t0), n);
-  return s * s >= lim * nn;
-}
-HD bool lb_reject_ee(d3 a0, d3 a1, d3 b0, d3 b1, double dhat) {
-  const double lim = dhat * (1.0 + 1e-6);
-  d3 u = sub(a1, a0), v = sub(b1, b0);
-  double uu = sqn(u), vv = sqn(v);
-  if (!(uu >= 1e-6 * dhat && vv >= 1e-6 * dhat)) return false;
-  d3 n = cross(u, v);
-  double nn = sqn(n);
-  if (!(nn >= 1e-6 * uu * vv)) return false;
-  d3 alo = vmin(a0, a1), ahi = vmax(a0, a1), blo = vmin(b0, b1), bhi = vmax(b0, b1);
-  double bx = dmax(0.0, dmax(alo.x - bhi.x, blo.x - ahi.x));
-  double by = dmax(0.0, dmax(alo.y - bhi.y, blo.y - ahi.y));
-  double bz = dmax(0.0, dmax(alo.z - bhi.z, blo.z - ahi.z));
-  if (bx * bx + by * by + bz * bz >= lim) return true;
-  double s = dot(sub(b0, a0), n);
-  return s * s >= lim * nn;
-}
-
-// ---------------------------------------------------------------------------------
 // Cubic roots in [x0, x1] by Yuksel's isolate-then-Newton method (HPG 2022), as the
 // reference uses it (cyCodeBase/cyPolynomial.h:787 with xError 6e-7). The bracketed
 // refinement loop that the published method leaves unbounded is capped here; the cap

@@ -358,14 +358,12 @@ __device__ __forceinline__ int exact_pair(const Geo& g, const Params& P, int sub
     box bv = inflate(box{p, p}, P.d_sqrt);
     d3 t0 = ldX(g.X, nv, g.fv[3 * pb]), t1 = ldX(g.X, nv, g.fv[3 * pb + 1]), t2 = ldX(g.X, nv, g.fv[3 * pb + 2]);
     if (!overlaps(bv, box3(t0, t1, t2))) return 0;
-    if (lb_reject_pt(p, t0, t1, t2, P.dhat)) return 0;
     int ty = pt_type(p, t0, t1, t2);
     return (pt_dist(p, t0, t1, t2, ty) < P.dhat) ? 1 + ty : 0;
   }
   d3 a0 = ldX(g.X, nv, g.ev[2 * pa]), a1 = ldX(g.X, nv, g.ev[2 * pa + 1]);
   d3 b0 = ldX(g.X, nv, g.ev[2 * pb]), b1 = ldX(g.X, nv, g.ev[2 * pb + 1]);
   if (!overlaps(inflate(box2(a0, a1), P.d_sqrt), box2(b0, b1))) return 0;
-  if (lb_reject_ee(a0, a1, b0, b1, P.dhat)) return 0;
   int ty = ee_type(a0, a1, b0, b1);
   return (ee_dist(a0, a1, b0, b1, ty) < P.dhat) ? 1 + ty : 0;
 }
@@ -481,8 +479,10 @@ __device__ __forceinline__ float lb2_ee_f(const float* a0, const float* a1, cons
 }
 
 // Rejects a float-box hit when the float lower bound of its squared distance reaches
-// dhat (1 + 1e-4) and the primitive is well shaped (the guards of lb_reject_pt/ee, so
-// the FP64 distance is accurate there): such a pair is one the FP64 test rejects too.
+// dhat (1 + 1e-4) and the primitives are well shaped (no edge with squared length below
+// 2e-6 dhat, no triangle or edge pair with |n|^2 below 2e-6 of the product of the squared
+// edge lengths, so the FP64 distance formulas are accurate far inside the 1e-4 margin):
+// such a pair is one the FP64 test rejects too, so it never reaches that test.
 __device__ __forceinline__ bool f_reject(const Geo& g, const float* vb, int sub, int pa, int pb, float lim) {
   const float *x0, *x1, *x2, *x3;
   if (sub < 2) {

@@ -525,9 +525,9 @@ __global__ void k_seg(int nov, int n, const int* pov, int* seg) {
   seg[u] = lo;
 }
 
-// Per-overlap sums of the pair records: 8 warps, each owns components c = w + 8k;
-// lanes stride over the overlap's pairs; fixed shuffle tree.
-__global__ void __launch_bounds__(256) k_ov_reduce(int nov, const int* pt_seg, const int* ee_seg, const double* ptC,
+// Per-overlap sums of the pair records: one CTA per overlap, one thread per record entry
+// (CONTRIB of them, one pass with 512 threads), each adding the overlap's pairs in order.
+__global__ void __launch_bounds__(512) k_ov_reduce(int nov, const int* pt_seg, const int* ee_seg, const double* ptC,
                                                    int npt, const double* eeC, int nee, double* ovr, int* has,
                                                    double off_scale) {
   int u = blockIdx.x;
@@ -1893,7 +1893,7 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
   if (nov) {
     KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, npt, S.pt_ov.p, B.pt_seg.p));
     KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, nee, S.ee_ov.p, B.ee_seg.p));
-    KLAUNCH(K_OV_REDUCE, s, k_ov_reduce<<<nov, 256, 0, s>>>(nov, B.pt_seg.p, B.ee_seg.p, B.pt_c.p, npt, B.ee_c.p, nee, B.ovr.p, B.has.p,
+    KLAUNCH(K_OV_REDUCE, s, k_ov_reduce<<<nov, 512, 0, s>>>(nov, B.pt_seg.p, B.ee_seg.p, B.pt_c.p, npt, B.ee_c.p, nee, B.ovr.p, B.has.p,
                                                                 P.damp ? 1 + P.damp_beta : 1.0));
   }
   KLAUNCH(K_BODY_SYSTEM, s, k_body_system<<<nb, 160, 0, s>>>(g, P, S.row_ptr.p, S.col.p, S.upidx.p, B.ovr.p, B.has.p, S.vg.p, S.vg_seg.p,
