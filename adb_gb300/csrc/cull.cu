@@ -332,9 +332,10 @@ constexpr int REC_CAP = 2048;  // accepted pairs of one overlap kept in shared m
 __host__ __device__ constexpr int narrow_step(int mode) { return mode == 2 ? 36 : 64; }
 __host__ __device__ constexpr int narrow_qcap(int mode) { return NT * narrow_step(mode); }
 // dynamic shared memory of k_narrow_scan<MODE>: boxes, queue, accepted pairs (MODE 0)
+// (MODE 0 also stages the vertex ids of the staged primitives: 2 per A entry, 3 per B)
 __host__ __device__ constexpr size_t narrow_smem(int mode) {
   return 2 * TILE * 6 * sizeof(float) + narrow_qcap(mode) * sizeof(unsigned) +
-         (mode == 0 ? REC_CAP * (sizeof(unsigned long long) + 1) : 0);
+         (mode == 0 ? REC_CAP * (sizeof(unsigned long long) + 1) + 5 * TILE * sizeof(int) : 0);
 }
 
 __device__ __forceinline__ void finflate(const float* s, float ds, float* o) {
@@ -351,21 +352,36 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
 // Exact narrow-phase test of one candidate at the culled configuration (vtn 1/2):
 // returns 0 (no pair) or 1 + distance type. sub 0/1: vertex v (global) of body A vs
 // face f (global) of body B; sub 2: edge ea vs edge eb.
-__device__ __forceinline__ int exact_pair(const Geo& g, const Params& P, int sub, int pa, int pb) {
+// The candidate is given by its four vertex ids: (point, triangle) for sub 0/1, (edge a,
+// edge b) for sub 2.
+__device__ __forceinline__ int exact_pair_v(const Geo& g, const Params& P, int sub, int v0, int v1, int v2, int v3) {
   int nv = g.nv;
   if (sub < 2) {
-    d3 p = ldX(g.X, nv, pa);
+    d3 p = ldX(g.X, nv, v0);
     box bv = inflate(box{p, p}, P.d_sqrt);
-    d3 t0 = ldX(g.X, nv, g.fv[3 * pb]), t1 = ldX(g.X, nv, g.fv[3 * pb + 1]), t2 = ldX(g.X, nv, g.fv[3 * pb + 2]);
+    d3 t0 = ldX(g.X, nv, v1), t1 = ldX(g.X, nv, v2), t2 = ldX(g.X, nv, v3);
     if (!overlaps(bv, box3(t0, t1, t2))) return 0;
     int ty = pt_type(p, t0, t1, t2);
     return (pt_dist(p, t0, t1, t2, ty) < P.dhat) ? 1 + ty : 0;
   }
-  d3 a0 = ldX(g.X, nv, g.ev[2 * pa]), a1 = ldX(g.X, nv, g.ev[2 * pa + 1]);
-  d3 b0 = ldX(g.X, nv, g.ev[2 * pb]), b1 = ldX(g.X, nv, g.ev[2 * pb + 1]);
+  d3 a0 = ldX(g.X, nv, v0), a1 = ldX(g.X, nv, v1);
+  d3 b0 = ldX(g.X, nv, v2), b1 = ldX(g.X, nv, v3);
   if (!overlaps(inflate(box2(a0, a1), P.d_sqrt), box2(b0, b1))) return 0;
   int ty = ee_type(a0, a1, b0, b1);
   return (ee_dist(a0, a1, b0, b1, ty) < P.dhat) ? 1 + ty : 0;
+}
+// Vertex ids of candidate (pa, pb): point pa and face pb (sub 0/1), edges pa and pb (sub 2).
+__device__ __forceinline__ void pair_vertex_ids(const Geo& g, int sub, int pa, int pb, int (&v)[4]) {
+  if (sub < 2) {
+    v[0] = pa; v[1] = g.fv[3 * pb]; v[2] = g.fv[3 * pb + 1]; v[3] = g.fv[3 * pb + 2];
+  } else {
+    v[0] = g.ev[2 * pa]; v[1] = g.ev[2 * pa + 1]; v[2] = g.ev[2 * pb]; v[3] = g.ev[2 * pb + 1];
+  }
+}
+__device__ __forceinline__ int exact_pair(const Geo& g, const Params& P, int sub, int pa, int pb) {
+  int v[4];
+  pair_vertex_ids(g, sub, pa, pb, v);
+  return exact_pair_v(g, P, sub, v[0], v[1], v[2], v[3]);
 }
 
 // ---- FP32 lower bounds of pair distances with tracked rounding errors ----
@@ -483,16 +499,9 @@ __device__ __forceinline__ float lb2_ee_f(const float* a0, const float* a1, cons
 // 2e-6 dhat, no triangle or edge pair with |n|^2 below 2e-6 of the product of the squared
 // edge lengths, so the FP64 distance formulas are accurate far inside the 1e-4 margin):
 // such a pair is one the FP64 test rejects too, so it never reaches that test.
-__device__ __forceinline__ bool f_reject(const Geo& g, const float* vb, int sub, int pa, int pb, float lim) {
-  const float *x0, *x1, *x2, *x3;
-  if (sub < 2) {
-    const int* f = g.fv + 3 * pb;
-    x0 = vb + 6 * pa; x1 = vb + 6 * f[0]; x2 = vb + 6 * f[1]; x3 = vb + 6 * f[2];
-  } else {
-    const int* ea = g.ev + 2 * pa;
-    const int* eb = g.ev + 2 * pb;
-    x0 = vb + 6 * ea[0]; x1 = vb + 6 * ea[1]; x2 = vb + 6 * eb[0]; x3 = vb + 6 * eb[1];
-  }
+// The candidate is given by its four vertex ids, as for exact_pair_v.
+__device__ __forceinline__ bool f_reject_v(const float* vb, int sub, int v0, int v1, int v2, int v3, float lim) {
+  const float *x0 = vb + 6 * v0, *x1 = vb + 6 * v1, *x2 = vb + 6 * v2, *x3 = vb + 6 * v3;
   // well-shaped guards in plain float with twice the FP64 guards' margins
   float ea[3], eb[3];
   for (int c = 0; c < 3; ++c) {
@@ -653,20 +662,43 @@ __global__ void k_refine(Geo g, float ds, int nov, const int* ovI, const int* ov
 
 // Stages one chunk of each list's float boxes in shared memory (A side inflated by
 // sqrt(dhat), rounded outward, unless `traj`).
-__device__ __forceinline__ void stage(const SubLists& L, int a0, int ca, int b0, int cb, bool inflate_a, float ds_f,
-                                      float* sA, float* sB) {
+// With sVA / sVB (pair cull) it also stages the vertex ids of the chunk's primitives:
+// A entry k at sVA[2k] (a point: its id; an edge: its two), B entry k at sVB[3k] (a face:
+// its three; an edge: its two), so the exact phase reads them from shared memory.
+__device__ __forceinline__ void stage(const Geo& g, int sub, const SubLists& L, int a0, int ca, int b0, int cb,
+                                      bool inflate_a, float ds_f, float* sA, float* sB, int* sVA, int* sVB) {
   __syncthreads();
   for (int k = threadIdx.x; k < ca; k += blockDim.x) {
-    const float* src = L.boxA + 6 * (L.offA + L.LA[a0 + k]);
+    const int pa = L.offA + L.LA[a0 + k];
+    const float* src = L.boxA + 6 * pa;
     if (inflate_a) finflate(src, ds_f, sA + 6 * k);
     else
 #pragma unroll
       for (int c = 0; c < 6; ++c) sA[6 * k + c] = src[c];
+    if (sVA) {
+      if (sub < 2) {
+        sVA[2 * k] = pa;
+      } else {
+        sVA[2 * k] = g.ev[2 * pa];
+        sVA[2 * k + 1] = g.ev[2 * pa + 1];
+      }
+    }
   }
   for (int k = threadIdx.x; k < cb; k += blockDim.x) {
-    const float* src = L.boxB + 6 * (L.offB + L.LB[b0 + k]);
+    const int pb = L.offB + L.LB[b0 + k];
+    const float* src = L.boxB + 6 * pb;
 #pragma unroll
     for (int c = 0; c < 6; ++c) sB[6 * k + c] = src[c];
+    if (sVB) {
+      if (sub < 2) {
+        sVB[3 * k] = g.fv[3 * pb];
+        sVB[3 * k + 1] = g.fv[3 * pb + 1];
+        sVB[3 * k + 2] = g.fv[3 * pb + 2];
+      } else {
+        sVB[3 * k] = g.ev[2 * pb];
+        sVB[3 * k + 1] = g.ev[2 * pb + 1];
+      }
+    }
   }
   __syncthreads();
 }
@@ -719,7 +751,9 @@ __global__ void __launch_bounds__(NT, MODE == 2 ? 3 : 2) k_narrow_scan(Geo g, Pa
   float* sB = sA + TILE * 6;
   unsigned int* sq = reinterpret_cast<unsigned int*>(sB + TILE * 6);
   constexpr int STEP = narrow_step(MODE);
-  int8_t* recT = reinterpret_cast<int8_t*>(sq + narrow_qcap(MODE));                         // REC_CAP (MODE 0)
+  int8_t* recT = reinterpret_cast<int8_t*>(sq + narrow_qcap(MODE));
+  int* sVA = MODE == 0 ? reinterpret_cast<int*>(recT + REC_CAP) : nullptr;  // 2 * TILE (MODE 0)
+  int* sVB = MODE == 0 ? sVA + 2 * TILE : nullptr;                           // 3 * TILE (MODE 0)                         // REC_CAP (MODE 0)
   __shared__ int sq_n[2];
   __shared__ int rec_n, rec_base;
   const int u = order[blockIdx.x];
@@ -747,7 +781,7 @@ __global__ void __launch_bounds__(NT, MODE == 2 ? 3 : 2) k_narrow_scan(Geo g, Pa
 #pragma unroll 1
       for (int b0 = 0; b0 < L.nB; b0 += TILE) {
         const int cb = min(TILE, L.nB - b0);
-        stage(L, a0, ca, b0, cb, MODE != 2, ds_f, sA, sB);
+        stage(g, sub, L, a0, ca, b0, cb, MODE != 2, ds_f, sA, sB, sVA, sVB);
         // thread t: rows i = t mod ca (ca < NT) or t, t + NT, ... (ca >= NT); columns
         // j = ph, ph + phases, ... with phases = NT / ca threads sharing a row
         const int rows = ca < NT ? ca : NT;
@@ -799,11 +833,15 @@ __global__ void __launch_bounds__(NT, MODE == 2 ? 3 : 2) k_narrow_scan(Geo g, Pa
             unsigned code = sq[k];
             int i = (int)(code >> 16), j = (int)(code & 0xffffu);
             if (i >= ca || j >= cb) continue;
-            int pa = L.offA + L.LA[a0 + i], pb = L.offB + L.LB[b0 + j];
             if (MODE == 2) {
+              int pa = L.offA + L.LA[a0 + i], pb = L.offB + L.LB[b0 + j];
               tmin = dmin(tmin, exact_toi(g, sub, pa, pb));
             } else {
-              int f = f_reject(g, vb, sub, pa, pb, lim_f) ? 0 : exact_pair(g, P, sub, pa, pb);
+              const int w0 = sVA[2 * i];
+              const int w1 = sub < 2 ? sVB[3 * j] : sVA[2 * i + 1];
+              const int w2 = sub < 2 ? sVB[3 * j + 1] : sVB[3 * j];
+              const int w3 = sub < 2 ? sVB[3 * j + 2] : sVB[3 * j + 1];
+              int f = f_reject_v(vb, sub, w0, w1, w2, w3, lim_f) ? 0 : exact_pair_v(g, P, sub, w0, w1, w2, w3);
               if (f) {
                 ++cs;
                 int slot = atomicAdd(&rec_n, 1);
