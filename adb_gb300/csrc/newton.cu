@@ -376,6 +376,23 @@ __global__ void __launch_bounds__(32 * MOLL_W) k_pair_moll(Geo g, Params P, int 
   }
 }
 
+// Per-pair body-space record (structure of arrays, stride = pairs): the two diagonal
+// blocks as upper triangles (78 entries each, row-major over row <= col), the
+// off-diagonal block (144, row-major, block (I, J)) and the two gradients (12 each).
+enum { PC_DJ = 78, PC_OFF = 156, PC_GI = 300, PC_GJ = 312, PAIRC = 324 };
+__host__ __device__ constexpr int sym12(int i, int j) { return i * 12 - (i * (i - 1)) / 2 + (j - i); }  // i <= j
+// upper-triangle index of entry (row, col) = e / 12, e % 12 of a symmetric 12 x 12 block
+struct Sym12Table {
+  unsigned char v[144];
+  constexpr Sym12Table() : v() {
+    for (int e = 0; e < 144; ++e) {
+      const int i = e / 12, j = e % 12;
+      v[e] = (unsigned char)(i <= j ? sym12(i, j) : sym12(j, i));
+    }
+  }
+};
+__constant__ Sym12Table c_sym12 = Sym12Table();
+
 // Per-pair terms, part 2: the chain rule onto the 12 affine DOFs of the two bodies,
 // d_A = Y_A S Y_A^T, d_B = Y_B S Y_B^T, off = Y_A S Y_B^T with Y_b[k][a] = sum over the
 // pair's vertices i on body b of xbar~_i[k] Q[i][a], and the body gradients.
@@ -394,20 +411,20 @@ __global__ void __launch_bounds__(128) k_pair_chain(Geo g, int kind, int n, cons
   const bool a_is_I = (A == I);
   const bool a_dyn = g.mass[A] > 0.0, b_dyn = g.mass[B] > 0.0;
   double* dI = C;
-  double* dJ = C + 144 * N;
-  double* off = C + 288 * N;
-  double* gI = C + 432 * N;
-  double* gJ = C + 444 * N;
+  double* dJ = C + PC_DJ * N;
+  double* off = C + PC_OFF * N;
+  double* gI = C + PC_GI * N;
+  double* gJ = C + PC_GJ * N;
   double* dA = a_is_I ? dI : dJ;
   double* dB = a_is_I ? dJ : dI;
   double* gA = a_is_I ? gI : gJ;
   double* gB = a_is_I ? gJ : gI;
   if (R[REC_ACT * N + p] == 0.0) {
-    for (int e = 0; e < 144; ++e) {
+    for (int e = 0; e < 78; ++e) {
       dI[e * N + p] = 0.0;
       dJ[e * N + p] = 0.0;
-      off[e * N + p] = 0.0;
     }
+    for (int e = 0; e < 144; ++e) off[e * N + p] = 0.0;
     for (int e = 0; e < 12; ++e) {
       gI[e * N + p] = 0.0;
       gJ[e * N + p] = 0.0;
@@ -475,12 +492,9 @@ __global__ void __launch_bounds__(128) k_pair_chain(Geo g, int kind, int n, cons
           if (r < s || k <= l) {
             double aa_ = TA[k][0] * YA[l][0] + TA[k][1] * YA[l][1] + TA[k][2] * YA[l][2];
             double bb_ = TB[k][0] * YB[l][0] + TB[k][1] * YB[l][1] + TB[k][2] * YB[l][2];
-            dA[e * N + p] = a_dyn ? aa_ : 0.0;
-            dB[e * N + p] = b_dyn ? bb_ : 0.0;
-            if (e != et) {
-              dA[et * N + p] = a_dyn ? aa_ : 0.0;
-              dB[et * N + p] = b_dyn ? bb_ : 0.0;
-            }
+            const int ui = c_sym12.v[e];  // the same entry for the whole warp
+            dA[ui * N + p] = a_dyn ? aa_ : 0.0;
+            dB[ui * N + p] = b_dyn ? bb_ : 0.0;
           }
           // (A row (k, r), B column (l, s)), stored as block (I, J)
           double ab_ = TA[k][0] * YB[l][0] + TA[k][1] * YB[l][1] + TA[k][2] * YB[l][2];
@@ -537,7 +551,7 @@ __global__ void __launch_bounds__(512) k_ov_reduce(int nov, const int* pt_seg, c
   if (p1 == p0 && e1 == e0) return;  // no pairs: the record is never read (has[u] = 0)
   // one thread per record entry, summing the overlap's pairs in order (each thread streams
   // its own component row; no FP64 shuffle tree, which costs more than the sums on GB300)
-  for (int c = threadIdx.x; c < CONTRIB; c += blockDim.x) {
+  for (int c = threadIdx.x; c < PAIRC; c += blockDim.x) {
     double s = 0.0;
     const double* pr = ptC + (size_t)c * npt;
     const double* er = eeC + (size_t)c * nee;
@@ -559,8 +573,22 @@ __global__ void __launch_bounds__(512) k_ov_reduce(int nov, const int* pt_seg, c
       s += a3;
     }
     for (; e < e1; ++e) s += er[e];
-    // the off-diagonal block takes the damping scale (1 + beta), like every matrix entry
-    ovr[(size_t)u * CONTRIB + c] = (c >= 288 && c < 432) ? s * off_scale : s;
+    // into the overlap record (CONTRIB layout: dI, dJ, off as full 12 x 12 blocks, gI,
+    // gJ); a diagonal-block entry fills both of its mirrored positions; the off-diagonal
+    // block takes the damping scale (1 + beta), like every matrix entry
+    double* o = ovr + (size_t)u * CONTRIB;
+    if (c < PC_OFF) {
+      const int blk = c < PC_DJ ? 0 : 144, t = c < PC_DJ ? c : c - PC_DJ;
+      int i = 0;
+      while (sym12(i, 11) < t) ++i;
+      const int j = i + (t - sym12(i, i));
+      o[blk + 12 * i + j] = s;
+      o[blk + 12 * j + i] = s;
+    } else if (c < PC_GI) {
+      o[288 + (c - PC_OFF)] = s * off_scale;
+    } else {
+      o[432 + (c - PC_GI)] = s;
+    }
   }
 }
 
@@ -1837,8 +1865,8 @@ __global__ void k_copy(double* d, const double* s, int n) {
 
 void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStream_t s) {
   int nb = g.nb, npt = S.npt, nee = S.nee, nov = S.nov;
-  B.pt_c.ensure((size_t)CONTRIB * npt + 1);
-  B.ee_c.ensure((size_t)CONTRIB * nee + 1);
+  B.pt_c.ensure((size_t)PAIRC * npt + 1);
+  B.ee_c.ensure((size_t)PAIRC * nee + 1);
   S.pt_lag.ensure(11 * (size_t)npt + 1);
   S.ee_lag.ensure(11 * (size_t)nee + 1);
   S.vg_lam.ensure((size_t)S.nvg + 1);
