@@ -101,6 +101,7 @@ struct Params {
 // Culling scratch shared by all culls of a handle.
 struct CullScratch {
   DBuf<double> bbox;
+  DBuf<float> bbox_f;  // body boxes in float, rounded outward
   DBuf<int> cnt_all, cnt_up, up_ptr, rowid;
   DBuf<double> ovcull;
   DBuf<float> ovcull_f;

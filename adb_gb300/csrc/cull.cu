@@ -60,7 +60,7 @@ __global__ void k_project(Geo g, int which, double alpha) {
 }
 
 // 2. body boxes
-__global__ void k_body_boxes(Geo g, int vtn, double alpha, double* bbox) {
+__global__ void k_body_boxes(Geo g, int vtn, double alpha, double* bbox, float* fbox) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= g.nb) return;
   box r{mk(g.rest_box[6 * b], g.rest_box[6 * b + 1], g.rest_box[6 * b + 2]),
@@ -78,14 +78,26 @@ __global__ void k_body_boxes(Geo g, int vtn, double alpha, double* bbox) {
   else o = merge(affine_box(r, q), affine_box(r, qt));
   bbox[6 * b] = o.lo.x; bbox[6 * b + 1] = o.lo.y; bbox[6 * b + 2] = o.lo.z;
   bbox[6 * b + 3] = o.hi.x; bbox[6 * b + 4] = o.hi.y; bbox[6 * b + 5] = o.hi.z;
+  // the same box in float, rounded outward: a float miss is an exact miss
+  fbox[6 * b] = __double2float_rd(o.lo.x); fbox[6 * b + 1] = __double2float_rd(o.lo.y);
+  fbox[6 * b + 2] = __double2float_rd(o.lo.z); fbox[6 * b + 3] = __double2float_ru(o.hi.x);
+  fbox[6 * b + 4] = __double2float_ru(o.hi.y); fbox[6 * b + 5] = __double2float_ru(o.hi.z);
+}
+
+// Float overlap of body boxes i and j (closed intervals, like intersection()).
+__device__ __forceinline__ bool fbox_meet(const float* fb, int i, int j) {
+  const float* a = fb + 6 * i;
+  const float* b = fb + 6 * j;
+  return a[0] <= b[3] && a[3] >= b[0] && a[1] <= b[4] && a[4] >= b[1] && a[2] <= b[5] && a[5] >= b[2];
 }
 
 __device__ __forceinline__ box ldbox(const double* bb, int i) {
   return box{mk(bb[6 * i], bb[6 * i + 1], bb[6 * i + 2]), mk(bb[6 * i + 3], bb[6 * i + 4], bb[6 * i + 5])};
 }
 
-// 3. overlaps: one warp per body row i, j over its scene (j != i), in increasing j.
-__global__ void k_ov_count(Geo g, const double* bbox, int* cnt_all, int* cnt_up) {
+// 3. overlaps: one warp per body row i, j over its scene (j != i), in increasing j; the
+// FP64 intersection runs only where the outward-rounded float boxes meet.
+__global__ void k_ov_count(Geo g, const double* bbox, const float* fbb, int* cnt_all, int* cnt_up) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= g.nb) return;
   int i = warp;
@@ -98,7 +110,7 @@ __global__ void k_ov_count(Geo g, const double* bbox, int* cnt_all, int* cnt_up)
   for (int j0 = g.scene_beg[i]; j0 < g.scene_end[i]; j0 += 32) {
     int j = j0 + lane;
     bool hit = false;
-    if (j < g.scene_end[i] && j != i) {
+    if (j < g.scene_end[i] && j != i && fbox_meet(fbb, i, j)) {
       box c;
       hit = intersection(bi, ldbox(bbox, j), c);
     }
@@ -113,8 +125,8 @@ __global__ void k_ov_count(Geo g, const double* bbox, int* cnt_all, int* cnt_up)
   }
 }
 
-__global__ void k_ov_fill(Geo g, const double* bbox, const int* row_ptr, const int* up_ptr, int* col, int* rowid,
-                          int* upidx, int* ovI, int* ovJ, double* ovcull, float* ovcull_f) {
+__global__ void k_ov_fill(Geo g, const double* bbox, const float* fbb, const int* row_ptr, const int* up_ptr, int* col,
+                          int* rowid, int* upidx, int* ovI, int* ovJ, double* ovcull, float* ovcull_f) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= g.nb) return;
   int i = warp;
@@ -126,7 +138,7 @@ __global__ void k_ov_fill(Geo g, const double* bbox, const int* row_ptr, const i
     int j = j0 + lane;
     bool hit = false;
     box c;
-    if (j < g.scene_end[i] && j != i) hit = intersection(bi, ldbox(bbox, j), c);
+    if (j < g.scene_end[i] && j != i && fbox_meet(fbb, i, j)) hit = intersection(bi, ldbox(bbox, j), c);
     unsigned m = __ballot_sync(0xffffffffu, hit);
     unsigned mu = __ballot_sync(0xffffffffu, hit && j > i);
     if (hit) {
@@ -1159,13 +1171,15 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
   }
   // 2-3. body boxes and overlaps
   cs.bbox.ensure(6 * (size_t)nb);
+  cs.bbox_f.ensure(6 * (size_t)nb);
   cs.cnt_all.ensure(nb + 1);
   cs.cnt_up.ensure(nb + 1);
   cs.up_ptr.ensure(nb + 1);
   PairSet& S = out;
   S.row_ptr.ensure(nb + 1);
-  KLAUNCH(K_BODY_BOXES, s, k_body_boxes<<<nblk(nb, 128), 128, 0, s>>>(g, vtn, alpha, cs.bbox.p));
-  KLAUNCH(K_OV_COUNT, s, k_ov_count<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, cs.cnt_all.p, cs.cnt_up.p));
+  KLAUNCH(K_BODY_BOXES, s, k_body_boxes<<<nblk(nb, 128), 128, 0, s>>>(g, vtn, alpha, cs.bbox.p, cs.bbox_f.p));
+  KLAUNCH(K_OV_COUNT, s, k_ov_count<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, cs.bbox_f.p, cs.cnt_all.p,
+                                                                                  cs.cnt_up.p));
   cs.tmp_int.ensure(64);
   int* d_tot = cs.tmp_int.p;  // [0] nnz, [1] nov, [2] list entries, [3] PT, [4] EE, [5] VG, [6] staged
   scan_exclusive_int(cs.cnt_all.p, S.row_ptr.p, nb, d_tot, s, cs.vflag_cnt);
@@ -1186,7 +1200,7 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
   S.ovJ.ensure(nov + 1);
   cs.ovcull.ensure(6 * (size_t)nov + 6);
   cs.ovcull_f.ensure(6 * (size_t)nov + 6);
-  KLAUNCH(K_OV_FILL, s, k_ov_fill<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, S.row_ptr.p, cs.up_ptr.p, S.col.p,
+  KLAUNCH(K_OV_FILL, s, k_ov_fill<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, cs.bbox_f.p, S.row_ptr.p, cs.up_ptr.p, S.col.p,
                                                           cs.rowid.p, S.upidx.p, S.ovI.p, S.ovJ.p, cs.ovcull.p,
                                                           cs.ovcull_f.p));
   if (nnz) {

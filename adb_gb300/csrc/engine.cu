@@ -132,7 +132,7 @@ struct Engine {
       S.pt.release(); S.ee.release(); S.pt_ty.release(); S.ee_ty.release(); S.pt_ov.release(); S.ee_ov.release();
       S.vg.release(); S.vg_seg.release(); S.pt_lag.release(); S.ee_lag.release(); S.vg_lam.release();
     }
-    cs.bbox.release(); cs.cnt_all.release(); cs.cnt_up.release(); cs.up_ptr.release(); cs.rowid.release();
+    cs.bbox.release(); cs.bbox_f.release(); cs.cnt_all.release(); cs.cnt_up.release(); cs.up_ptr.release(); cs.rowid.release();
     cs.ovcull.release(); cs.ovcull_f.release(); cs.vbox.release(); cs.ebox.release(); cs.fbox.release();
     cs.order.release(); cs.order_cnt.release();
     cs.bin_cnt.release(); cs.bin_off.release(); cs.lst.release(); cs.cand_cnt.release(); cs.cand_off.release();
