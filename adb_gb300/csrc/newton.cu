@@ -1716,12 +1716,17 @@ __global__ void __launch_bounds__(256) k_energy(Geo g, Params P, EnergyArgs a) {
   }
 }
 
+// Scene totals of the chunk partials: one warp per scene, lane l adding chunks l, l + 32,
+// ... in order, then a fixed shuffle tree (a serial sum by one thread was a chain of
+// hundreds of dependent FP64 adds).
 __global__ void k_scene_energy(int ns, const int* chunk_off, const double* part, double* out) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (s >= ns) return;
   double t = 0.0;
-  for (int c = chunk_off[s]; c < chunk_off[s + 1]; ++c) t += part[c];
-  out[s] = t;
+  for (int c = chunk_off[s] + lane; c < chunk_off[s + 1]; c += 32) t += part[c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) out[s] = t;
 }
 
 // Per scene: dq.grad, |grad|^2, |dq|^2 (one block per scene; thread t takes the scene's
@@ -2084,7 +2089,7 @@ void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet&
   prof_work(K_ENERGY, (double)a.npt + a.nee + a.lpt + a.lee,
             136.0 * ((double)a.npt + a.nee + a.lpt + a.lee) + 96.0 * g.nb);
   KLAUNCH(K_ENERGY, s, k_energy<<<G, 256, 0, s>>>(g, P, a));
-  KLAUNCH(K_ENERGY, s, k_scene_energy<<<nblk(ns, 128), 128, 0, s>>>(ns, B.e_chunk_off.p, B.red.p, B.e_out.p));
+  KLAUNCH(K_ENERGY, s, k_scene_energy<<<nblk(32ll * ns, 128), 128, 0, s>>>(ns, B.e_chunk_off.p, B.red.p, B.e_out.p));
   CK(cudaMemcpyAsync(out, B.e_out.p, ns * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
 }
