@@ -890,9 +890,13 @@ __global__ void __launch_bounds__(NT, MODE == 2 ? 3 : 2) k_narrow_scan(Geo g, Pa
     // Sort the collected (sub, i, j) keys (bitonic, shared memory) and stage them, so
     // the write pass only copies. Overlaps with more pairs than REC_CAP are marked
     // (stage_off = -1) and written by the recomputing pass instead.
+    // stage_total[1] counts the overlaps left to the recomputing pass
     int nr = rec_n;
     if (nr > REC_CAP || nr == 0) {
-      if (threadIdx.x == 0) stage_off[u] = (nr == 0) ? 0 : -1;
+      if (threadIdx.x == 0) {
+        stage_off[u] = (nr == 0) ? 0 : -1;
+        if (nr) atomicAdd(stage_total + 1, 1);
+      }
       return;
     }
     int np2 = 1;
@@ -920,6 +924,7 @@ __global__ void __launch_bounds__(NT, MODE == 2 ? 3 : 2) k_narrow_scan(Geo g, Pa
       int base = atomicAdd(stage_total, nr);
       rec_base = (base + nr <= stage_cap) ? base : -2;
       stage_off[u] = rec_base;
+      if (rec_base < 0) atomicAdd(stage_total + 1, 1);
     }
     __syncthreads();
     if (rec_base >= 0)
@@ -1181,7 +1186,8 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
   KLAUNCH(K_OV_COUNT, s, k_ov_count<<<nblk((long long)nb * 32, 256), 256, 0, s>>>(g, cs.bbox.p, cs.bbox_f.p, cs.cnt_all.p,
                                                                                   cs.cnt_up.p));
   cs.tmp_int.ensure(64);
-  int* d_tot = cs.tmp_int.p;  // [0] nnz, [1] nov, [2] list entries, [3] PT, [4] EE, [5] VG, [6] staged
+  int* d_tot = cs.tmp_int.p;  // [0] nnz, [1] nov, [2] list entries, [3] PT, [4] EE, [5] VG, [6] staged,
+                              // [7] overlaps left to the recomputing write pass
   scan_exclusive_int(cs.cnt_all.p, S.row_ptr.p, nb, d_tot, s, cs.vflag_cnt);
   scan_exclusive_int(cs.cnt_up.p, cs.up_ptr.p, nb, d_tot + 1, s, cs.vflag_cnt);
   // the vertex-ground pairs need only the positions: counted now, read with the overlaps
@@ -1302,7 +1308,7 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
                                                                                        cs.vbox.p, cs.ebox.p, cs.fbox.p));
     order_overlaps(nov, cs, s, K_NARROW_SCAN);
     for (int attempt = 0; attempt < 4; ++attempt) {
-      CK(cudaMemsetAsync(d_tot + 6, 0, sizeof(int), s));
+      CK(cudaMemsetAsync(d_tot + 6, 0, 2 * sizeof(int), s));
       narrow_smem_attr();
       KLAUNCH(K_NARROW_SCAN, s, k_narrow_scan<0><<<nov, NT, narrow_smem(0), s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
                                                                       cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
@@ -1313,7 +1319,7 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
       KLAUNCH(K_NARROW_WRITE, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
       scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
       scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
-      CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 5 * sizeof(int), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       if ((size_t)cs.h_small[6] <= cs.stage_key.cap) break;
       // staging overflowed: grow to the reported total and classify again
@@ -1333,10 +1339,11 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
     KLAUNCH(K_NARROW_WRITE, s, k_narrow_copy<<<nov, 128, 0, s>>>(nov, S.ovI.p, S.ovJ.p, cs.bin_off.p, cs.lst.p,
                                                                   cs.sub_cnt.p, cs.stage_key.p, cs.stage_ty.p,
                                                                   cs.stage_off.p, cs.blk_a_off.p, cs.blk_b_off.p, no));
-    KLAUNCH(K_NARROW_WRITE, s, k_narrow_write<<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
-                                                                  cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
-                                                                  cs.fbox.p, cs.sub_cnt.p, cs.blk_a_off.p,
-                                                                  cs.blk_b_off.p, no, cs.stage_off.p));
+    if (cs.h_small[7] > 0)  // some overlap was not staged: the recomputing pass writes it
+      KLAUNCH(K_NARROW_WRITE, s, k_narrow_write<<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
+                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
+                                                                    cs.fbox.p, cs.sub_cnt.p, cs.blk_a_off.p,
+                                                                    cs.blk_b_off.p, no, cs.stage_off.p));
   }
   S.npt = npt;
   S.nee = nee;

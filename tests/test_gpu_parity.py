@@ -85,6 +85,19 @@ def test_cull_bit_exact_sphere_pile(O):
     assert_sets_equal(g, o)
 
 
+def test_cull_bit_exact_dense_overlap(O):
+    # two near-coincident spheres: a single overlap with more pairs than the narrow phase
+    # keeps in shared memory (2048), so the recomputing write pass produces it
+    sc = S.sphere_pile(2, 1, 1, subdiv=2, jitter=0.0, vel_sigma=0.0, seed=3)
+    q = sc.q0.copy()
+    q[1, :3] = q[0, :3] + np.array([0.004, 0.003, -0.002])
+    cfg = S.workload_config("pile")
+    gpu, orc = ABD(sc, cfg), O.OracleSim(sc, cfg)
+    g, o = gpu.cull(1, q), orc.cull(1, q)
+    assert len(o[0]) + len(o[2]) > 2048
+    assert_sets_equal(g, o)
+
+
 def test_distance_types_and_tois_bit_exact(O):
     rng = np.random.default_rng(4)
     X = rng.normal(size=(3000, 4, 3)) * 0.02
