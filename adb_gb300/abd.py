@@ -118,6 +118,13 @@ class ABD:
     def set_friction(self, mu: float):
         L.check(L.lib().abd_set_friction(self._h, float(mu)), self._h, "abd_set_friction")
 
+    @property
+    def friction(self) -> float:
+        """The handle's current friction coefficient (config "mu" or the last set_friction)."""
+        mu = C.c_double(0.0)
+        L.check(L.lib().abd_get_friction(self._h, C.byref(mu)), self._h, "abd_get_friction")
+        return mu.value
+
     def adjoint_frame(self, q_t: np.ndarray, v_t: np.ndarray, q_next: np.ndarray, gq_next: np.ndarray):
         """(dL/dq_t, dL/dv_t, dL/dmu) of one converged frame from dL/dq_{t+1}."""
         a = [np.ascontiguousarray(x, np.float64) for x in (q_t, v_t, q_next, gq_next)]

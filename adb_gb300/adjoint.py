@@ -39,12 +39,26 @@ class Rollout(torch.autograd.Function):
                 ckpt[t + 1] = sim.state()
         qT, vT = sim.state()
         ckpt[n_steps] = (qT.copy(), vT.copy())
-        ctx.sim, ctx.n, ctx.ckpt = sim, n_steps, ckpt
+        ctx.sim, ctx.n, ctx.ckpt, ctx.mu = sim, n_steps, ckpt, float(mu)
         return torch.from_numpy(qT.copy()), torch.from_numpy(vT.copy())
 
     @staticmethod
     def backward(ctx, gqT, gvT):
         sim, n, ckpt = ctx.sim, ctx.n, ctx.ckpt
+        # The simulation may have run other rollouts (another mu, another state) since this
+        # forward pass: recompute and differentiate with this rollout's friction, and hand
+        # the simulation back as it was found.
+        saved_state, saved_mu, saved_iter = sim.state(), sim.friction, sim.iter
+        sim.set_friction(ctx.mu)
+        try:
+            return Rollout._backward(ctx, sim, n, ckpt, gqT, gvT)
+        finally:
+            sim.set_friction(saved_mu)
+            sim.set_state(*saved_state)
+            sim.iter = saved_iter
+
+    @staticmethod
+    def _backward(ctx, sim, n, ckpt, gqT, gvT):
         dt = sim.config.dt
         shape = ckpt[0][0].shape
         gq = np.zeros(shape) if gqT is None else gqT.detach().cpu().numpy().astype(np.float64).copy()

@@ -564,7 +564,7 @@ struct abd_handle {
 };
 
 namespace {
-std::string g_last_error;
+thread_local std::string g_last_error;  // errors of calls without a handle, per host thread
 
 struct ProfScope {
   abd::Prof* prev;
@@ -850,6 +850,12 @@ int abd_set_friction(abd_handle* h, double mu) {
   if (!h || !(mu >= 0.0)) return ABD_ERR_INVALID;
   h->e.P.mu = mu;
   h->e.cfg.mu = mu;
+  return ABD_OK;
+}
+
+int abd_get_friction(abd_handle* h, double* mu) {
+  if (!h || !mu) return ABD_ERR_INVALID;
+  *mu = h->e.P.mu;
   return ABD_OK;
 }
 

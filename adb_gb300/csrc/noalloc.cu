@@ -12,9 +12,13 @@
 // The scratch array below is a device symbol: every GPU that loads the library holds it
 // until the process exits. Host code must not pass its name to a kernel (on the host it
 // is only a stand-in, not a device address); its device address is looked up once per
-// device with cudaGetSymbolAddress and cached. Every call shares the array: calls that
+// device with cudaGetSymbolAddress and cached. The cache assumes one CUDA context per
+// device for the life of the process: after cudaDeviceReset (or any teardown that
+// re-creates the primary context) the cached address is stale, so a process that resets
+// a device must not call this entry point again. Every call shares the array: calls that
 // overlap on the GPU (different streams, or different host threads on one device) race
-// on it and must be serialised by the caller.
+// on it and must be serialised by the caller. The error message is kept per host thread,
+// so concurrent failing calls never write to one string.
 #include <mutex>
 #include <string>
 
@@ -33,7 +37,7 @@ static __device__ __align__(256) double g_noalloc_partial[NOALLOC_MAX_BLOCKS];
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 double* g_noalloc_ptr[kMaxDevices] = {};
-std::string g_noalloc_err;
+thread_local std::string g_noalloc_err;  // last error of the calling host thread
 
 __device__ __forceinline__ d3 ld(const double* x, int i) { return mk(x[3 * i], x[3 * i + 1], x[3 * i + 2]); }
 

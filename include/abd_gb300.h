@@ -123,6 +123,7 @@ int abd_get_iter(abd_handle* h);
 int abd_set_iter(abd_handle* h, int iter);
 /* Friction coefficient of the handle (config "mu"), e.g. between differentiated rollouts. */
 int abd_set_friction(abd_handle* h, double mu);
+int abd_get_friction(abd_handle* h, double* mu);
 /* Adjoint of one converged frame (no reference counterpart: the reference has no
  * derivatives). The frame maps the frame-start state (q_t, v_t) and mu to q_{t+1}; given
  * gq_next = dL/dq_{t+1} it assembles the exact Jacobian of the frame's optimality condition
@@ -138,6 +139,8 @@ int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const
  * cumulative Newton counter. */
 int abd_get_scene_count(abd_handle* h);
 int abd_get_scene_stats(abd_handle* h, int* newton_iters, int* ls_trials, int* pcg_iters, int* iter);
+/* Message of the handle's last error; with h = NULL, of the last failing call without a
+ * handle (abd_create*) made by the calling host thread. */
 const char* abd_last_error(abd_handle* h);
 void abd_destroy(abd_handle* h);
 /* Per-kernel device timing: when enabled, every kernel of the step is bracketed with
@@ -191,6 +194,7 @@ int abd_ee_distance_batch(int n, const double* x, int* type, double* dist);
  * `stream` (a cudaStream_t, NULL = default stream); the call does not synchronise. */
 #define ABD_NOALLOC_MAX_N (1 << 22)
 int abd_pt_min_toi_noalloc(int n, const double* d_x, double* d_toi, double* d_min, void* stream);
+/* Message of the last failing abd_pt_min_toi_noalloc call made by the calling host thread. */
 const char* abd_noalloc_last_error(void);
 
 /* Dense FP64 FMA throughput of this GPU in GFLOP/s (roofline denominator for the

@@ -80,3 +80,43 @@ def test_adjoint_matches_oracle_finite_differences(O, mu, contact_friction, boun
               oracle_loss(O, sc, cfg, sc.q0, v0, mu - h, target, n)) / (2 * h)
         print("adjoint mu: %.10g fd %.10g" % (float(mut.grad), fd))
         assert abs(float(mut.grad) - fd) <= bound * abs(fd), (float(mut.grad), fd)
+
+
+def test_interleaved_rollouts_keep_their_own_friction(gpu_lib):
+    """Two rollouts of one simulation with different mu, then backward on their summed
+    loss: each backward pass recomputes its frames (checkpoints every 4) with its own mu,
+    so the gradients equal those of each rollout differentiated alone, and the simulation
+    is handed back with the state and friction it had."""
+    from adb_gb300.abd import ABD
+    from adb_gb300.adjoint import rollout
+    sc, cfg, target, v0 = setup(0.2, contact_friction=False)
+    n = 8
+    tgt = torch.tensor(target)
+
+    def grads(mus, together):
+        sim = ABD(sc, cfg)
+        out = []
+        losses = []
+        for mu in mus:
+            v0t = torch.tensor(v0, dtype=torch.float64, requires_grad=True)
+            mut = torch.tensor(mu, dtype=torch.float64, requires_grad=True)
+            qT, _ = rollout(sim, torch.tensor(sc.q0), v0t, mut, n, every=4)
+            loss = ((qT[:, :3] - tgt) ** 2).sum()
+            if together:
+                losses.append(loss)
+            else:
+                loss.backward()
+            out.append((v0t, mut))
+        if together:
+            before = sim.state(), sim.friction
+            sum(losses).backward()
+            after = sim.state(), sim.friction
+            assert after[1] == before[1]
+            assert np.array_equal(after[0][0], before[0][0]) and np.array_equal(after[0][1], before[0][1])
+        sim.close()
+        return [(v.grad.numpy().copy(), float(m.grad)) for v, m in out]
+
+    alone = grads([0.0, 0.3], together=False)
+    both = grads([0.0, 0.3], together=True)
+    for (ga, ma), (gb, mb) in zip(alone, both):
+        assert np.array_equal(ga, gb) and ma == mb
