@@ -28,7 +28,8 @@ class AbdConfig(C.Structure):
             "clip", "pcg_max_iter", "iaabb", "full_ccd")] + [(n, C.c_double) for n in (
                 "safe_factor", "sh_min_xyz", "sh_dx")] + [(n, C.c_int) for n in (
                     "sh_xyz_bits", "sh_fix_edge_trajectory")] + [("dq_tol", C.c_double), ("damping", C.c_int),
-                                                                 ("damp_alpha", C.c_double), ("damp_beta", C.c_double)]
+                                                                 ("damp_alpha", C.c_double), ("damp_beta", C.c_double),
+                                                                 ("pcg_refine", C.c_int), ("pcg_refine_tol", C.c_double)]
 
 
 class AbdSceneDesc(C.Structure):
@@ -81,6 +82,7 @@ def lib():
         L.abd_get_pairs.argtypes = [H, _I, _I, _I, _I, _I]
         L.abd_newton_system.argtypes = [H, _D, _D, _D, _I, _I, _D, C.c_int]
         L.abd_newton_dq.argtypes = [H, _D, _D, _I]
+        L.abd_energy.argtypes = [H, _D, _D, _D, _I, _D, _D, _D, _D, _D, _D]
         L.abd_ipc_hess_pt_batch.argtypes = [C.c_int, _D, _I, _D, C.c_double, C.c_double, C.c_int, _D, _D]
         L.abd_ipc_hess_ee_batch.argtypes = [C.c_int, _D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, _D,
                                             _D, _D]
@@ -103,7 +105,7 @@ def lib():
 # Every symbol include/abd_gb300.h declares (checked by the CPU test suite).
 EXPORTED = ["abd_create", "abd_create_from_files", "abd_step", "abd_get_state", "abd_set_state", "abd_get_counts",
             "abd_get_iter", "abd_set_iter", "abd_get_scene_count", "abd_get_scene_stats", "abd_set_friction", "abd_get_friction", "abd_adjoint_frame", "abd_last_error", "abd_destroy", "abd_profile", "abd_kernel_times", "abd_kernel_work", "abd_cull", "abd_get_pairs",
-            "abd_newton_system", "abd_newton_dq", "abd_ipc_hess_pt_batch", "abd_ipc_hess_ee_batch",
+            "abd_newton_system", "abd_newton_dq", "abd_energy", "abd_ipc_hess_pt_batch", "abd_ipc_hess_ee_batch",
             "abd_pt_collision_time_batch", "abd_ee_collision_time_batch", "abd_pt_distance_batch",
             "abd_ee_distance_batch", "abd_pt_min_toi_noalloc", "abd_noalloc_last_error", "abd_measure_fp64_gflops"]
 

@@ -31,6 +31,7 @@ def make_abd_config(cfg: Config) -> L.AbdConfig:
     c.sh_min_xyz, c.sh_dx, c.sh_xyz_bits = cfg.sh_min_xyz, cfg.sh_dx, int(cfg.sh_bits)
     c.sh_fix_edge_trajectory, c.dq_tol = int(cfg.sh_fix_edge_trajectory), cfg.dq_tol
     c.damping, c.damp_alpha, c.damp_beta = int(cfg.damping), cfg.damp_alpha, cfg.damp_beta
+    c.pcg_refine, c.pcg_refine_tol = int(cfg.pcg_refine), cfg.pcg_refine_tol
     return c
 
 
@@ -202,6 +203,27 @@ class ABD:
         L.check(lib.abd_newton_system(self._h, L.dptr(q), L.dptr(grad), L.dptr(diag), C.byref(n), L.iptr(keys),
                                       L.dptr(vals), k), self._h, "abd_newton_system")
         return grad, diag, keys[:n.value], vals[:n.value]
+
+    def energy(self, q: np.ndarray, dq: np.ndarray) -> dict:
+        """Line-search energy at q + dq with the friction lagged at q (the first trial of the
+        reference's line search at alpha = 1, abd_energy): per-scene `terms` (inertia +
+        orthogonality, PT, EE and ground barrier, friction, the line-search total), pair
+        `counts`, per-pair barrier energies (e_pt, e_ee, e_vg) of the set at q + dq and
+        friction energies (f_pt, f_ee, f_vg) of the lagged set."""
+        lib = L.lib()
+        q = np.ascontiguousarray(q, np.float64)
+        dq = np.ascontiguousarray(dq, np.float64)
+        cnt = np.zeros(6, np.int32)
+        L.check(lib.abd_energy(self._h, L.dptr(q), L.dptr(dq), None, L.iptr(cnt), None, None, None, None, None,
+                               None), self._h, "abd_energy")
+        terms = np.zeros((self.n_scenes, 6))
+        arr = [np.zeros(max(int(n), 1)) for n in cnt]
+        L.check(lib.abd_energy(self._h, L.dptr(q), L.dptr(dq), L.dptr(terms), L.iptr(cnt), *[L.dptr(a) for a in arr]),
+                self._h, "abd_energy")
+        out = {k: a[:int(n)] for k, a, n in zip(("e_pt", "e_ee", "e_vg", "f_pt", "f_ee", "f_vg"), arr, cnt)}
+        out["terms"] = terms
+        out["counts"] = cnt
+        return out
 
     def newton_dq(self, q: np.ndarray):
         q = np.ascontiguousarray(q, np.float64)

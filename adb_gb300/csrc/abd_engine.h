@@ -245,6 +245,9 @@ struct NewtonBufs {
   DBuf<int> e_off, e_chunk_cnt, e_chunk_off, e_scan_tmp;
   DBuf<double> e_out;        // per-scene energies / dot products
   DBuf<int> status;          // [0] solver status, [1] pcg iters
+  DBuf<double> xr, rt, dqc;  // iterative refinement: accumulated solution, true residual, -d
+  DBuf<int> it_ref;          // refinement: [0] total iterations, [2 + k] per scene
+  std::vector<int> h_ref;
   double* h_red = nullptr;   // pinned
   int* h_int = nullptr;
 };
@@ -254,12 +257,19 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& nb, cudaStr
 // Body groups of the PCG (consecutive bodies of one scene, cut from the scene's first
 // body); called once per handle with the scenes' body ranges.
 void pcg_groups(const std::vector<int>& sc_beg, const std::vector<int>& sc_end, NewtonBufs& nb, cudaStream_t s);
+// refine > 0: that many iterative-refinement passes, each solving H d = b - H x (true
+// residual) by the same PCG to refine_tol relative and adding d to x.
 int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& nb, double rel_tol, int max_iter, const int* sc_on, double* dq,
-              cudaStream_t s, int* status, int* scene_iters);
+              cudaStream_t s, int* status, int* scene_iters, int refine = 0, double refine_tol = 1e-8);
 // Line-search energy of every scene at the trial configuration (X must hold q + alpha dq):
 // inertia + barrier over `Snew` + lagged friction over `Slag`; out (host) receives ns values.
 void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_barrier_inertia,
             NewtonBufs& nb, cudaStream_t s, double* out);
+// Every term of that energy on its own, into device array `out`: the bodies' inertia +
+// orthogonality (nb), the barrier energies of Snew's PT, EE, VG pairs, then the friction
+// energies of Slag's PT, EE, VG pairs, in list order.
+void energy_terms(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, double* out,
+                  cudaStream_t s);
 // Per scene over its 12 n dofs: out[3s] = dq.grad, out[3s+1] = |grad|^2, out[3s+2] = |dq|^2
 void dots(const Geo& g, const double* dq, const double* grad, NewtonBufs& nb, double* out, cudaStream_t s);
 // Per scene: out[3s] = a.b, out[3s+1] = |b|^2, out[3s+2] = |a - b|^2

@@ -156,6 +156,7 @@ struct Engine {
     nbufs.sc_conv.release(); nbufs.sc_iters.release(); nbufs.n_active.release();
     nbufs.e_off.release(); nbufs.e_chunk_cnt.release(); nbufs.e_chunk_off.release(); nbufs.e_scan_tmp.release();
     nbufs.e_out.release(); nbufs.red.release(); nbufs.status.release();
+    nbufs.xr.release(); nbufs.rt.release(); nbufs.dqc.release(); nbufs.it_ref.release();
     if (nbufs.h_red) cudaFreeHost(nbufs.h_red);
     if (nbufs.h_int) cudaFreeHost(nbufs.h_int);
     if (h_on) cudaFreeHost(h_on);
@@ -399,7 +400,8 @@ struct Engine {
       st.bytes_moved += bytes_assemble(S);
       auto t1 = clk::now();
       int pst = 0;
-      int its = pcg_solve(g, S, nbufs, cfg.pcg_rel_tol, cfg.pcg_max_iter, sc_on.p, dq.p, s, &pst, its_s.data());
+      int its = pcg_solve(g, S, nbufs, cfg.pcg_rel_tol, cfg.pcg_max_iter, sc_on.p, dq.p, s, &pst, its_s.data(),
+                          cfg.pcg_refine, cfg.pcg_refine_tol);
       st.pcg_iters += its;
       for (int k = 0; k < ns; ++k) sc_pcg[k] += its_s[k];
       st.bytes_moved += its * (1152.0 * (nb + 2.0 * S.nov) + 6 * 96.0 * nb) + 1152.0 * nb;
@@ -846,6 +848,73 @@ int abd_newton_system(abd_handle* h, const double* q, double* grad, double* diag
   });
 }
 
+// Line-search energy terms at q + dq with the friction lagged at q: the quantities of the
+// first trial of ABD::line_search at alpha = 1 (line_search.cpp:88-110; E_barrier_plus_inert
+// energy.cpp:19-86, E_fric :195-258, E_ground :261-270).
+int abd_energy(abd_handle* h, const double* q, const double* dq, double* terms, int* counts, double* e_pt,
+               double* e_ee, double* e_vg, double* f_pt, double* f_ee, double* f_vg) {
+  if (!h || !q || !dq) return ABD_ERR_INVALID;
+  return guarded(h, [&]() {
+    Engine& e = h->e;
+    const int nb = e.nb, ns = e.ns;
+    const size_t n = 12 * (size_t)nb;
+    newton_system_at(e, q);  // culls at q and assembles there: the lagged friction of that set
+    abd::PairSet& L = e.sets[e.cur];
+    abd::PairSet& T = e.sets[1 - e.cur];
+    CK(cudaMemcpyAsync(e.dq.p, dq, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
+    abd::Geo g = e.geo();
+    e.cull_set(g, 2, T, 1.0);  // the set at q + dq; positions at q + dq stay in X
+    std::vector<double> tot(ns);
+    abd::energy(g, e.P, 1.0, T, L, true, e.nbufs, e.s, tot.data());
+    const int c[6] = {T.npt, T.nee, T.nvg, L.npt, L.nee, L.nvg};
+    size_t m = nb;
+    for (int k = 0; k < 6; ++k) m += c[k];
+    abd::DBuf<double> d_out;
+    d_out.ensure(m + 1);
+    abd::energy_terms(g, e.P, 1.0, T, L, d_out.p, e.s);
+    std::vector<double> v(m);
+    CK(cudaMemcpyAsync(v.data(), d_out.p, m * sizeof(double), cudaMemcpyDeviceToHost, e.s));
+    // scene of each listed pair: the scene of its first body
+    std::vector<int> lists[6];
+    const abd::PairSet* src[6] = {&T, &T, &T, &L, &L, &L};
+    for (int k = 0; k < 6; ++k) {
+      const int stride = (k % 3 == 2) ? 2 : 4;
+      const int* d = (k % 3 == 0) ? src[k]->pt.p : (k % 3 == 1) ? src[k]->ee.p : src[k]->vg.p;
+      lists[k].resize((size_t)stride * c[k]);
+      if (c[k]) CK(cudaMemcpyAsync(lists[k].data(), d, lists[k].size() * sizeof(int), cudaMemcpyDeviceToHost, e.s));
+    }
+    CK(cudaStreamSynchronize(e.s));
+    d_out.release();
+    std::vector<int> bsc(nb);
+    for (int k = 0; k < ns; ++k)
+      for (int b = e.h_sc_beg[k]; b < e.h_sc_end[k]; ++b) bsc[b] = k;
+    // terms per scene: inertia + orthogonality, PT, EE, ground barrier, friction, and the
+    // total as the line search sums it
+    if (terms) {
+      for (int k = 0; k < 6 * ns; ++k) terms[k] = 0.0;
+      for (int b = 0; b < nb; ++b) terms[6 * bsc[b]] += v[b];
+      size_t o = nb;
+      for (int k = 0; k < 6; ++k) {
+        const int stride = (k % 3 == 2) ? 2 : 4;
+        const int slot = k < 3 ? 1 + k : 4;
+        for (int i = 0; i < c[k]; ++i) terms[6 * bsc[lists[k][(size_t)stride * i]] + slot] += v[o + i];
+        o += c[k];
+      }
+      for (int k = 0; k < ns; ++k) terms[6 * k + 5] = tot[k];
+    }
+    double* outs[6] = {e_pt, e_ee, e_vg, f_pt, f_ee, f_vg};
+    size_t o = nb;
+    for (int k = 0; k < 6; ++k) {
+      if (outs[k]) std::memcpy(outs[k], v.data() + o, c[k] * sizeof(double));
+      o += c[k];
+    }
+    if (counts)
+      for (int k = 0; k < 6; ++k) counts[k] = c[k];
+    e.last_cull_set = 1 - e.cur;
+    return (int)ABD_OK;
+  });
+}
+
 int abd_set_friction(abd_handle* h, double mu) {
   if (!h || !(mu >= 0.0)) return ABD_ERR_INVALID;
   h->e.P.mu = mu;
@@ -897,7 +966,8 @@ int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const
     for (int it = 0; it < 50; ++it) {
       for (size_t k = 0; k < n; ++k) rhs[k] = gq_next[k] - ctw[k];
       CK(cudaMemcpyAsync(e.nbufs.grad.p, rhs.data(), n * sizeof(double), cudaMemcpyHostToDevice, e.s));
-      abd::pcg_solve(g, S, e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.sc_on.p, e.dq.p, e.s, &st, nullptr);
+      abd::pcg_solve(g, S, e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.sc_on.p, e.dq.p, e.s, &st, nullptr,
+                     e.cfg.pcg_refine, e.cfg.pcg_refine_tol);
       if (st == ABD_ERR_NOT_SPD) return st;
       wprev = w;
       CK(cudaMemcpyAsync(w.data(), e.nbufs.x.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
@@ -951,7 +1021,7 @@ int abd_newton_dq(abd_handle* h, const double* q, double* dq, int* pcg_iters) {
     int st = 0;
     e.put_on(std::vector<char>(e.ns, 1));
     int its = abd::pcg_solve(e.geo(), e.sets[e.cur], e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.sc_on.p,
-                             e.dq.p, e.s, &st, nullptr);
+                             e.dq.p, e.s, &st, nullptr, e.cfg.pcg_refine, e.cfg.pcg_refine_tol);
     if (pcg_iters) *pcg_iters = its;
     CK(cudaMemcpy(dq, e.dq.p, 12 * (size_t)e.nb * sizeof(double), cudaMemcpyDeviceToHost));
     return st;

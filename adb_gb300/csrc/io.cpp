@@ -243,6 +243,8 @@ extern "C" int abd_create_from_files(const char* config_json, const char* scene_
   c.ee_fric = cfgj.flag("ee_friction", true);
   c.clip = pi ? (int)pi->num("clip", 0) : 0;
   c.pcg_max_iter = (int)cfgj.num("pcg_max_iter", 5000);
+  c.pcg_refine = (int)cfgj.num("pcg_refine", 0);
+  c.pcg_refine_tol = cfgj.num("pcg_refine_tol", 1e-8);
   c.iaabb = (int)cfgj.num("iaabb", 3);
   c.full_ccd = cfgj.flag("full_ccd", true);
   c.safe_factor = cfgj.num("safe_factor", 1.0);

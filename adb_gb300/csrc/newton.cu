@@ -1716,6 +1716,13 @@ __global__ void __launch_bounds__(256) k_energy(Geo g, Params P, EnergyArgs a) {
   }
 }
 
+// Every term of one list on its own (the values k_energy sums): out[i] = term i of
+// segment seg (-1: bodies).
+__global__ void k_energy_each(Geo g, Params P, EnergyArgs a, int seg, int n, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = energy_term(g, P, a, seg, i);
+}
+
 // Scene totals of the chunk partials: one warp per scene, lane l adding chunks l, l + 32,
 // ... in order, then a fixed shuffle tree (a serial sum by one thread was a chain of
 // hundreds of dependent FP64 adds).
@@ -1844,6 +1851,44 @@ __global__ void k_spmv(int nb, const int* row_ptr, const int* col, const int* up
   y[12 * body + row] = row_spmv(a, body, row, x);
 }
 
+// True residual r = b - H x of the row-block system the PCG iterates on (one thread per
+// body row, the row's blocks in list order); bodies of scenes that are not solved get 0.
+__global__ void k_true_residual(int nb, const int* row_ptr, const int* rcol, const int* rn, const double* Hrow,
+                                const int* bscene, const int* sc_on, const double* b, const double* x, double* r) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int body = t / 12, row = t - 12 * body;
+  if (body >= nb) return;
+  if (!sc_on[bscene[body]]) {
+    r[t] = 0.0;
+    return;
+  }
+  const int base = body + row_ptr[body], n = rn[body];
+  double acc = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const double* H = Hrow + (size_t)(base + j) * 144 + 12 * row;
+    const double* v = x + 12 * rcol[base + j];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) acc = __fma_rn(H[c], v[c], acc);
+  }
+  r[t] = __dsub_rn(b[t], acc);
+}
+
+// Iteration counts of a refinement solve added to the running totals: acc[0] += the
+// solve's count (its longest scene), acc[2 + k] += scene k's.
+__global__ void k_iter_add(int ns, const int* its, const int* sc_its, int* acc) {
+  if (threadIdx.x == 0) acc[0] += its[0];
+  for (int k = threadIdx.x; k < ns; k += blockDim.x) acc[2 + k] += sc_its[k];
+}
+
+// x += d, dq = -x (a refinement step of the Newton solve)
+__global__ void k_refine_add(int n, double* x, const double* d, double* dq) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = __dadd_rn(x[i], d[i]);
+  x[i] = v;
+  dq[i] = -v;
+}
+
 // v *= f[scene of body]
 __global__ void k_scale_scene(double* v, int n, const int* bscene, const double* f) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1934,7 +1979,7 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
 }
 
 int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_iter, const int* sc_on, double* dq,
-              cudaStream_t s, int* status, int* scene_iters) {
+              cudaStream_t s, int* status, int* scene_iters, int refine, double refine_tol) {
   int nb = g.nb, ns = g.ns;
   B.status.ensure(4);
   if (!B.h_int) CK(cudaMallocHost(&B.h_int, 16 * sizeof(int)));
@@ -2012,11 +2057,48 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
   a.maxit = max_iter < 0 ? 0 : max_iter;
   a.out = B.status.p;
   void* args[] = {&a};
-  KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel(one ? (void*)k_pcg1 : (void*)k_pcg, dim3(grid), dim3(PCG_NT), args,
-                                                     0, s)));
-  CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
-  if (scene_iters) CK(cudaMemcpyAsync(scene_iters, B.sc_iters.p, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  const void* kern = one ? (void*)k_pcg1 : (void*)k_pcg;
+  KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(PCG_NT), args, 0, s)));
+  const int nrows = 12 * nb;
+  if (refine > 0) {
+    // Iterative refinement: the PCG's recurrence residual drifts from b - H x as the
+    // iterates converge, so the solution is corrected with the true residual computed
+    // from the same row-block matrix, each correction solved by the same PCG to
+    // refine_tol relative to its residual. The first iteration count is read with the
+    // corrections' (one host read at the end).
+    B.xr.ensure(nrows);
+    B.rt.ensure(nrows);
+    B.it_ref.ensure(2 * (size_t)ns + 2);
+    B.h_ref.resize(2 * (size_t)ns + 2);
+    CK(cudaMemcpyAsync(B.xr.p, B.x.p, nrows * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(B.it_ref.p, B.status.p + 1, sizeof(int), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(B.it_ref.p + 2, B.sc_iters.p, ns * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    PcgArgs c = a;
+    c.b = B.rt.p;
+    c.tol2 = refine_tol * refine_tol;
+    B.dqc.ensure(nrows);
+    c.dq = B.dqc.p;  // the correction's -d (unused)
+    void* cargs[] = {&c};
+    for (int k = 0; k < refine; ++k) {
+      KLAUNCH(K_PCG, s, k_true_residual<<<nblk(nrows, 256), 256, 0, s>>>(nb, S.row_ptr.p, B.rcol.p, B.rn.p,
+                                                                         B.Hrow.p, g.bscene, sc_on, B.grad.p,
+                                                                         B.xr.p, B.rt.p));
+      KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(PCG_NT), cargs, 0, s)));
+      KLAUNCH(K_VEC, s, k_refine_add<<<nblk(nrows, 256), 256, 0, s>>>(nrows, B.xr.p, B.x.p, dq));
+      KLAUNCH(K_VEC, s, k_iter_add<<<1, 32, 0, s>>>(ns, B.status.p + 1, B.sc_iters.p, B.it_ref.p));
+    }
+    CK(cudaMemcpyAsync(B.x.p, B.xr.p, nrows * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(B.h_ref.data(), B.it_ref.p, (2 + (size_t)ns) * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    B.h_int[1] = B.h_ref[0];
+    if (scene_iters)
+      for (int k = 0; k < ns; ++k) scene_iters[k] = B.h_ref[2 + k];
+  } else {
+    CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (scene_iters) CK(cudaMemcpyAsync(scene_iters, B.sc_iters.p, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
   *status = B.h_int[0];
   // per iteration: the kept blocks once (1152 B each) and ~6 vector streams
   prof_work(K_PCG, B.h_int[1], B.h_int[1] * (1152.0 * B.h_int[2] + 6 * 96.0 * nb) + 1152.0 * nb);
@@ -2046,8 +2128,7 @@ void pcg_groups(const std::vector<int>& sc_beg, const std::vector<int>& sc_end, 
   CK(cudaStreamSynchronize(s));
 }
 
-void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_bi, NewtonBufs& B,
-            cudaStream_t s, double* out) {
+static EnergyArgs energy_args(const Geo& g, double alpha, PairSet& Snew, PairSet& Slag, bool with_bi) {
   EnergyArgs a;
   a.nb = g.nb;
   a.ns = g.ns;
@@ -2070,6 +2151,27 @@ void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet&
   a.lpt_lag = Slag.pt_lag.p;
   a.lee_lag = Slag.ee_lag.p;
   a.lvg_lam = Slag.vg_lam.p;
+  a.off = nullptr;
+  a.chunk_off = nullptr;
+  a.partial = nullptr;
+  return a;
+}
+
+void energy_terms(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, double* out,
+                  cudaStream_t s) {
+  EnergyArgs a = energy_args(g, alpha, Snew, Slag, true);
+  const int n[1 + NSEG] = {g.nb, a.npt, a.nee, a.nvg, a.lpt, a.lee, a.lvg};
+  size_t o = 0;
+  for (int k = 0; k <= NSEG; ++k) {
+    if (n[k] > 0)
+      KLAUNCH(K_ENERGY, s, k_energy_each<<<nblk(n[k], 128), 128, 0, s>>>(g, P, a, k - 1, n[k], out + o));
+    o += n[k];
+  }
+}
+
+void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_bi, NewtonBufs& B,
+            cudaStream_t s, double* out) {
+  EnergyArgs a = energy_args(g, alpha, Snew, Slag, with_bi);
   const int ns = g.ns;
   B.e_off.ensure((size_t)NSEG * (ns + 1));
   B.e_chunk_cnt.ensure(ns + 1);

@@ -72,6 +72,8 @@ class Config:
     # GPU solver controls (no reference counterpart: the reference factorizes directly)
     pcg_rel_tol: float = 1e-14
     pcg_max_iter: int = 5000
+    pcg_refine: int = 0            # iterative-refinement passes after the PCG (true residual)
+    pcg_refine_tol: float = 1e-8   # relative tolerance of each correction solve
 
     @property
     def gravity_y(self) -> float:
@@ -130,6 +132,8 @@ def load_config(path: str) -> Config:
     c.solver = str(d.get("solver", c.solver))
     c.pcg_rel_tol = float(d.get("pcg_rel_tol", c.pcg_rel_tol))
     c.pcg_max_iter = int(d.get("pcg_max_iter", c.pcg_max_iter))
+    c.pcg_refine = int(d.get("pcg_refine", c.pcg_refine))
+    c.pcg_refine_tol = float(d.get("pcg_refine_tol", c.pcg_refine_tol))
     return c
 
 
@@ -150,6 +154,7 @@ def config_to_json(c: Config) -> dict:
         "params_int": {"clip": c.clip, "thres": 100},
         "dhat": c.dhat, "ortho_kappa": c.ortho_kappa, "ground_y": -c.ground_offset,
         "pcg_rel_tol": c.pcg_rel_tol, "pcg_max_iter": c.pcg_max_iter,
+        "pcg_refine": c.pcg_refine, "pcg_refine_tol": c.pcg_refine_tol,
     }
 
 

@@ -71,6 +71,12 @@ typedef struct {
   int damping;           /* "damping": {"enable"}: H (1 + beta) + diag(m, Ic) (alpha - beta)
                             (damping_sparse, mutils.cpp:106-115) */
   double damp_alpha, damp_beta;
+  /* Newton solve (the reference factorizes directly, abd.cpp:229-303): after the PCG,
+   * pcg_refine passes of iterative refinement, each solving H d = b - H x with the true
+   * residual to pcg_refine_tol relative and adding d, bring the solution to the backward
+   * error of a direct solve. */
+  int pcg_refine;
+  double pcg_refine_tol;
 } abd_config;
 
 /* Scene: bodies with their rest meshes (local vertex ids per body). */
@@ -164,6 +170,17 @@ int abd_get_pairs(abd_handle* h, int* pt, int* pt_type, int* ee, int* ee_type, i
  * blocks (144 nb, row-major), upper off-diagonal blocks (keys I<J, 144 each). */
 int abd_newton_system(abd_handle* h, const double* q, double* grad, double* diag, int* n_off, int* off_keys,
                       double* off_vals, int max_off);
+/* Line-search energy (E_barrier_plus_inert energy.cpp:19-86, E_fric :195-258, E_ground
+ * :261-270) at q + dq with the friction lagged at q, i.e. the first trial of
+ * ABD::line_search at alpha = 1 (line_search.cpp:88-110), with the handle's q0 / qdot as
+ * the frame start. Culls at q, assembles there (lagged tangent bases and multipliers),
+ * culls at q + dq and evaluates. terms (6 per scene, or NULL): inertia + orthogonality,
+ * point-triangle barrier, edge-edge barrier (mollified), ground barrier, friction, and the
+ * scene total as the line search sums it. counts (6, or NULL): pt, ee, vg pairs of the set
+ * at q + dq, then of the lagged set at q. Per-pair arrays (each NULL or sized by counts):
+ * barrier energies of the set at q + dq, friction energies of the lagged set. */
+int abd_energy(abd_handle* h, const double* q, const double* dq, double* terms, int* counts, double* e_pt,
+               double* e_ee, double* e_vg, double* f_pt, double* f_ee, double* f_vg);
 /* Newton step dq = -H^{-1} grad at state q (PCG). */
 int abd_newton_dq(abd_handle* h, const double* q, double* dq, int* pcg_iters);
 

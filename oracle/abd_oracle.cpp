@@ -1172,8 +1172,74 @@ static bool block_cholesky_solve(const BlockSys& sys, std::vector<double>& x) {
 }
 
 // ---------------------------------------------------------------------------------
-// Energies of the line search (energy.cpp:19-86, 195-270).
-static double E_barrier_plus_inert(Scene& s, const PairSet& P, const std::vector<double>& dqk) {
+// Energies of the line search (energy.cpp:19-86, 195-270), one function per term so the
+// totals and the per-pair values of orc_energy_terms come from the same arithmetic.
+// Positions are those of the last project_all (s.X at q + dq, s.X0 at q0).
+static double pt_barrier_energy(Scene& s, const I4& ij) {  // energy.cpp:34-50
+  V3 X[4];
+  X[0] = Xat(s, ij[0], ij[1]);
+  face_at(s, s.X, ij[2], ij[3], X + 1);
+  PTType t = pt_type(X[0], X[1], X[2], X[3]);
+  return barrier(pt_dist(X[0], X[1], X[2], X[3], t), s.bp);
+}
+static double ee_barrier_energy(Scene& s, const I4& ij) {  // energy.cpp:52-80, mollified
+  V3 X[4];
+  edge_at(s, s.X, ij[0], ij[1], X);
+  edge_at(s, s.X, ij[2], ij[3], X + 2);
+  double eps_x = sqnorm(X[0] - X[1]) * sqnorm(X[2] - X[3]) * s.cfg.eps_x;
+  double m;
+  V3 u = X[1] - X[0], v = X[3] - X[2];
+  double x = sqnorm(cross(u, v));
+  if (x < eps_x) {
+    double xe = x / eps_x;
+    m = (-xe + 2.0) * xe;
+  } else {
+    m = 1.0;
+  }
+  EEType t = ee_type(X[0], X[1], X[2], X[3]);
+  return barrier(ee_dist(X[0], X[1], X[2], X[3], t), s.bp) * m;
+}
+static double vg_barrier_energy(Scene& s, const std::array<int, 2>& iv) {  // E_ground, energy.cpp:261-270
+  V3 p = Xat(s, iv[0], iv[1]);
+  double d = p.y + s.cfg.ground_offset;
+  d = d * d;
+  return d < s.bp.dhat ? barrier(d, s.bp) : 0.0;
+}
+// Lagged friction of pair k of the current set (E_fric, energy.cpp:195-258): tangent
+// displacement Tk (x - x0) of the pair's four vertices.
+static double pair_friction_energy(Scene& s, int kind, int k) {
+  const I4& ij = kind ? s.set.ee[k] : s.set.pt[k];
+  V3 X[4], X0[4];
+  if (kind) {
+    edge_at(s, s.X, ij[0], ij[1], X);
+    edge_at(s, s.X, ij[2], ij[3], X + 2);
+    edge_at(s, s.X0, ij[0], ij[1], X0);
+    edge_at(s, s.X0, ij[2], ij[3], X0 + 2);
+  } else {
+    X[0] = Xat(s, ij[0], ij[1]);
+    face_at(s, s.X, ij[2], ij[3], X + 1);
+    X0[0] = s.X0[s.b[ij[0]].v_off + ij[1]];
+    face_at(s, s.X0, ij[2], ij[3], X0 + 1);
+  }
+  const auto& Tk = kind ? s.ee_tk[k] : s.pt_tk[k];
+  double u0 = 0, u1 = 0;
+  for (int i = 0; i < 4; ++i)
+    for (int r = 0; r < 3; ++r) {
+      double du = X[i][r] - X0[i][r];
+      u0 += Tk(0, 3 * i + r) * du;
+      u1 += Tk(1, 3 * i + r) * du;
+    }
+  double lam = kind ? s.ee_lam[k] : s.pt_lam[k];
+  return s.fp.mu * lam * f0_SF(std::sqrt(u0 * u0 + u1 * u1), s.fp.epsv);
+}
+static double vg_friction_energy(Scene& s, int k) {  // ground friction in the x, z plane
+  int I = s.set.vg[k][0], v = s.set.vg[k][1];
+  V3 d = s.X[s.b[I].v_off + v] - s.X0[s.b[I].v_off + v];
+  return s.fp.mu * s.g_lam[k] * f0_SF(std::sqrt(d.x * d.x + d.z * d.z), s.fp.epsv);
+}
+
+// Inertia + orthogonality of every body at q + dqk (the bodies' dq is set to dqk).
+static double E_inert(Scene& s, const std::vector<double>& dqk) {
   int nb = (int)s.b.size();
   double e = 0;
   for (int I = 0; I < nb; ++I) {
@@ -1183,50 +1249,23 @@ static double E_barrier_plus_inert(Scene& s, const PairSet& P, const std::vector
     q_plus(c.q, c.dq, q1);
     e += inertia_energy(s, c, q1);
   }
+  return e;
+}
+
+static double E_barrier_plus_inert(Scene& s, const PairSet& P, const std::vector<double>& dqk) {
+  double e = E_inert(s, dqk);
   project_all(s, 2);
   double ep = 0, ee_ = 0, eg = 0;
   if (s.cfg.pt) {
 #pragma omp parallel for reduction(+ : ep) schedule(static)
-    for (int k = 0; k < (int)P.pt.size(); ++k) {
-      const I4& ij = P.pt[k];
-      V3 X[4];
-      X[0] = Xat(s, ij[0], ij[1]);
-      face_at(s, s.X, ij[2], ij[3], X + 1);
-      PTType t = pt_type(X[0], X[1], X[2], X[3]);
-      ep += barrier(pt_dist(X[0], X[1], X[2], X[3], t), s.bp);
-    }
+    for (int k = 0; k < (int)P.pt.size(); ++k) ep += pt_barrier_energy(s, P.pt[k]);
   }
   if (s.cfg.ee) {
 #pragma omp parallel for reduction(+ : ee_) schedule(static)
-    for (int k = 0; k < (int)P.ee.size(); ++k) {
-      const I4& ij = P.ee[k];
-      V3 X[4];
-      edge_at(s, s.X, ij[0], ij[1], X);
-      edge_at(s, s.X, ij[2], ij[3], X + 2);
-      double eps_x = sqnorm(X[0] - X[1]) * sqnorm(X[2] - X[3]) * s.cfg.eps_x;
-      double m;
-      V12 gm;
-      M12 Hm;
-      V3 u = X[1] - X[0], v = X[3] - X[2];
-      double x = sqnorm(cross(u, v));
-      if (x < eps_x) {
-        double xe = x / eps_x;
-        m = (-xe + 2.0) * xe;
-      } else {
-        m = 1.0;
-      }
-      (void)gm; (void)Hm;
-      EEType t = ee_type(X[0], X[1], X[2], X[3]);
-      ee_ += barrier(ee_dist(X[0], X[1], X[2], X[3], t), s.bp) * m;
-    }
+    for (int k = 0; k < (int)P.ee.size(); ++k) ee_ += ee_barrier_energy(s, P.ee[k]);
   }
   if (s.cfg.ground) {
-    for (int k = 0; k < (int)P.vg.size(); ++k) {
-      V3 p = Xat(s, P.vg[k][0], P.vg[k][1]);
-      double d = p.y + s.cfg.ground_offset;
-      d = d * d;
-      if (d < s.bp.dhat) eg += barrier(d, s.bp);
-    }
+    for (int k = 0; k < (int)P.vg.size(); ++k) eg += vg_barrier_energy(s, P.vg[k]);
   }
   return e + ep + ee_ + eg;
 }
@@ -1238,51 +1277,16 @@ static double E_fric(Scene& s, const std::vector<double>& dqk) {
   project_all(s, 2);
   const PairSet& P = s.set;
   double ef = 0;
-  double mu = s.fp.mu, ev = s.fp.epsv;
   if (s.cfg.pt && s.cfg.pt_fric) {
 #pragma omp parallel for reduction(+ : ef) schedule(static)
-    for (int k = 0; k < (int)P.pt.size(); ++k) {
-      const I4& ij = P.pt[k];
-      V3 X[4], X0[4];
-      X[0] = Xat(s, ij[0], ij[1]);
-      face_at(s, s.X, ij[2], ij[3], X + 1);
-      X0[0] = s.X0[s.b[ij[0]].v_off + ij[1]];
-      face_at(s, s.X0, ij[2], ij[3], X0 + 1);
-      double u0 = 0, u1 = 0;
-      for (int i = 0; i < 4; ++i)
-        for (int r = 0; r < 3; ++r) {
-          double du = X[i][r] - X0[i][r];
-          u0 += s.pt_tk[k](0, 3 * i + r) * du;
-          u1 += s.pt_tk[k](1, 3 * i + r) * du;
-        }
-      ef += mu * s.pt_lam[k] * f0_SF(std::sqrt(u0 * u0 + u1 * u1), ev);
-    }
+    for (int k = 0; k < (int)P.pt.size(); ++k) ef += pair_friction_energy(s, 0, k);
   }
   if (s.cfg.ee && s.cfg.ee_fric) {
 #pragma omp parallel for reduction(+ : ef) schedule(static)
-    for (int k = 0; k < (int)P.ee.size(); ++k) {
-      const I4& ij = P.ee[k];
-      V3 X[4], X0[4];
-      edge_at(s, s.X, ij[0], ij[1], X);
-      edge_at(s, s.X, ij[2], ij[3], X + 2);
-      edge_at(s, s.X0, ij[0], ij[1], X0);
-      edge_at(s, s.X0, ij[2], ij[3], X0 + 2);
-      double u0 = 0, u1 = 0;
-      for (int i = 0; i < 4; ++i)
-        for (int r = 0; r < 3; ++r) {
-          double du = X[i][r] - X0[i][r];
-          u0 += s.ee_tk[k](0, 3 * i + r) * du;
-          u1 += s.ee_tk[k](1, 3 * i + r) * du;
-        }
-      ef += mu * s.ee_lam[k] * f0_SF(std::sqrt(u0 * u0 + u1 * u1), ev);
-    }
+    for (int k = 0; k < (int)P.ee.size(); ++k) ef += pair_friction_energy(s, 1, k);
   }
   if (s.cfg.ground && s.cfg.vg_fric) {
-    for (int k = 0; k < (int)P.vg.size(); ++k) {
-      int I = P.vg[k][0], v = P.vg[k][1];
-      V3 d = s.X[s.b[I].v_off + v] - s.X0[s.b[I].v_off + v];
-      ef += mu * s.g_lam[k] * f0_SF(std::sqrt(d.x * d.x + d.z * d.z), ev);
-    }
+    for (int k = 0; k < (int)P.vg.size(); ++k) ef += vg_friction_energy(s, k);
   }
   return ef;
 }
@@ -1586,6 +1590,74 @@ int orc_newton_dq(void* h, const double* q, double* dq) {
   std::vector<double> x;
   if (!block_cholesky_solve(sys, x)) return ST_NOT_SPD;
   for (size_t i = 0; i < x.size(); ++i) dq[i] = -x[i];
+  return 0;
+}
+
+// Line-search energy terms at q + dq with the friction lagged at q (the first trial of
+// ABD::line_search at alpha = 1, line_search.cpp:88-110): culls at q, assembles there
+// (lagged Tk, lambda), culls at q + dq, then evaluates.
+// terms: [inertia + orthogonality, PT barrier, EE barrier, ground barrier, friction];
+// counts: pairs of the set at q + dq (pt, ee, vg), then of the lagged set (pt, ee, vg);
+// per-pair arrays (any may be null): barrier energies over the set at q + dq, friction
+// energies over the lagged set (0 where the term is switched off).
+int orc_energy_terms(void* h, const double* q, const double* dq, double* terms, int* counts, double* e_pt,
+                     double* e_ee, double* e_vg, double* f_pt, double* f_ee, double* f_vg) {
+  Scene& s = *(Scene*)h;
+  int nb = (int)s.b.size();
+  for (int I = 0; I < nb; ++I) {
+    std::memcpy(s.b[I].q, q + 12 * I, 12 * sizeof(double));
+    std::memset(s.b[I].dq, 0, 12 * sizeof(double));
+  }
+  cull(s, 1, &s.set);
+  BlockSys sys;
+  assemble(s, sys);
+  std::vector<double> dqk(dq, dq + 12 * nb);
+  for (int I = 0; I < nb; ++I) std::memcpy(s.b[I].dq, dq + 12 * I, 12 * sizeof(double));
+  PairSet Pn;
+  cull(s, 2, &Pn);
+  double t[5] = {E_inert(s, dqk), 0, 0, 0, 0};
+  project_all(s, 2);
+  for (int k = 0; k < (int)Pn.pt.size(); ++k) {
+    double e = s.cfg.pt ? pt_barrier_energy(s, Pn.pt[k]) : 0.0;
+    if (e_pt) e_pt[k] = e;
+    t[1] += e;
+  }
+  for (int k = 0; k < (int)Pn.ee.size(); ++k) {
+    double e = s.cfg.ee ? ee_barrier_energy(s, Pn.ee[k]) : 0.0;
+    if (e_ee) e_ee[k] = e;
+    t[2] += e;
+  }
+  for (int k = 0; k < (int)Pn.vg.size(); ++k) {
+    double e = s.cfg.ground ? vg_barrier_energy(s, Pn.vg[k]) : 0.0;
+    if (e_vg) e_vg[k] = e;
+    t[3] += e;
+  }
+  const PairSet& L = s.set;
+  for (int k = 0; k < (int)L.pt.size(); ++k) {
+    double e = (s.cfg.pt && s.cfg.pt_fric) ? pair_friction_energy(s, 0, k) : 0.0;
+    if (f_pt) f_pt[k] = e;
+    t[4] += e;
+  }
+  for (int k = 0; k < (int)L.ee.size(); ++k) {
+    double e = (s.cfg.ee && s.cfg.ee_fric) ? pair_friction_energy(s, 1, k) : 0.0;
+    if (f_ee) f_ee[k] = e;
+    t[4] += e;
+  }
+  for (int k = 0; k < (int)L.vg.size(); ++k) {
+    double e = (s.cfg.ground && s.cfg.vg_fric) ? vg_friction_energy(s, k) : 0.0;
+    if (f_vg) f_vg[k] = e;
+    t[4] += e;
+  }
+  if (terms)
+    for (int i = 0; i < 5; ++i) terms[i] = t[i];
+  if (counts) {
+    counts[0] = (int)Pn.pt.size();
+    counts[1] = (int)Pn.ee.size();
+    counts[2] = (int)Pn.vg.size();
+    counts[3] = (int)L.pt.size();
+    counts[4] = (int)L.ee.size();
+    counts[5] = (int)L.vg.size();
+  }
   return 0;
 }
 

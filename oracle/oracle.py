@@ -62,6 +62,7 @@ def lib():
         L.orc_get_pairs.argtypes = [C.c_void_p, _I, _I, _I, _I, _I]
         L.orc_newton_system.argtypes = [C.c_void_p, _D, _D, _D, _I, _D, C.c_int]
         L.orc_newton_dq.argtypes = [C.c_void_p, _D, _D]
+        L.orc_energy_terms.argtypes = [C.c_void_p, _D, _D, _D, _I, _D, _D, _D, _D, _D, _D]
         L.orc_energy.restype = C.c_double
         L.orc_energy.argtypes = [C.c_void_p, _D]
         L.orc_stats_last.argtypes = [C.c_void_p, C.POINTER(OracleStats)]
@@ -207,6 +208,21 @@ class OracleSim:
         if rc:
             raise RuntimeError("oracle solve failed: status %d" % rc)
         return dq
+
+    def energy_terms(self, q: np.ndarray, dq: np.ndarray) -> dict:
+        """Line-search energy at q + dq with the friction lagged at q (orc_energy_terms)."""
+        q = np.ascontiguousarray(q, np.float64)
+        dq = np.ascontiguousarray(dq, np.float64)
+        cnt = np.zeros(6, np.int32)
+        terms = np.zeros(5)
+        lib().orc_energy_terms(self.h, _d(q), _d(dq), _d(terms), _i(cnt), None, None, None, None, None, None)
+        arr = [np.zeros(max(int(n), 1)) for n in cnt]
+        lib().orc_energy_terms(self.h, _d(q), _d(dq), _d(terms), _i(cnt), *[_d(a) for a in arr])
+        names = ("e_pt", "e_ee", "e_vg", "f_pt", "f_ee", "f_vg")
+        out = {k: a[:int(n)] for k, a, n in zip(names, arr, cnt)}
+        out["terms"] = terms
+        out["counts"] = cnt
+        return out
 
     def energy(self, q: np.ndarray) -> float:
         q = np.ascontiguousarray(q, np.float64)

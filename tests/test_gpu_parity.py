@@ -1,8 +1,19 @@
 """GPU path (libabd_gb300.so, called through the C ABI) against the CPU oracle.
 
-Bar: pair sets and distance types bit-exact; TOIs bit-exact; per-pair energy, gradient
-and Hessian within 1e-9 relative; Newton systems within 1e-9 relative; per-frame
-states within 1e-9 relative (relative to the largest state entry)."""
+Bar: pair sets and distance types bit-exact; TOIs bit-exact; per-pair gradient and
+Hessian within 1e-9 relative; Newton systems and Newton steps within 1e-9 relative;
+per-frame states from the same start state within 1e-9 relative (relative to the largest
+state entry). Per-pair and per-scene energies are checked in test_gpu_energy.py.
+
+A frame of the reference step can amplify rounding-level differences: on a frame with
+dozens of Newton iterations and line-search steps of a few 1e-3, the oracle itself moves
+by ~1e-9 when its start state is perturbed by 1e-16 relative. No implementation with a
+different rounding (another summation order, FMA, a different solver) can agree with it
+below that level. So a frame that misses 1e-9 passes only if the oracle's own measured
+sensitivity on that frame is above 1e-10 and the GPU error is within SENS_FACTOR of it;
+every other frame must meet 1e-9."""
+import os
+
 import numpy as np
 import pytest
 
@@ -12,6 +23,7 @@ from adb_gb300 import scene as S
 pytestmark = pytest.mark.gpu
 
 REL = 1e-9
+SENS_FACTOR = 10.0   # GPU error allowed on an ill-conditioned frame, in units of the oracle's own sensitivity
 
 
 def rel(a, b):
@@ -166,7 +178,24 @@ def test_newton_system_matches_oracle(O):
     if len(ov):
         assert rel(gv, ov) <= REL
     gdq, its = gpu.newton_dq(q)
-    assert rel(gdq, orc_dq(O, sc, cfg, q0, qd, q)) <= 1e-7
+    assert rel(gdq, orc_dq(O, sc, cfg, q0, qd, q)) <= REL
+
+
+def test_newton_steps_match_direct_solve_on_pile_frames(O):
+    """The block-Jacobi PCG step against the oracle's direct block-sparse Cholesky (the
+    reference factorizes, abd.cpp:229-303) on ten contact-rich frames of a small pile."""
+    sc = S.sphere_pile(3, 3, 2, subdiv=1, seed=2)
+    cfg = S.workload_config("pile")
+    orc = O.OracleSim(sc, cfg)
+    orc.step(20)
+    gpu = ABD(sc, cfg)
+    for _ in range(10):
+        orc.step(1)
+        q0, qd = orc.state()
+        gpu.set_state(q0, qd)
+        gdq, its = gpu.newton_dq(q0)
+        assert its > 0
+        assert rel(gdq, orc_dq(O, sc, cfg, q0, qd, q0)) <= REL
 
 
 def orc_system(O, sc, cfg, q0, qd, q):
@@ -181,15 +210,21 @@ def orc_dq(O, sc, cfg, q0, qd, q):
     return o.newton_dq(q)
 
 
-def run_pair(O, sc, cfg, frames):
+def run_pair(O, sc, cfg, frames, start=None, gpu=None):
     """Steps both implementations frame by frame; before every frame the GPU state is
     reset to the oracle's, so each comparison is one frame from the same start state.
-    Returns the per-frame relative state differences. Newton and line-search counts
-    (the discrete decisions of the step) must match on every frame."""
-    gpu, orc = ABD(sc, cfg), O.OracleSim(sc, cfg)
-    errs = []
+    Returns the per-frame relative state differences and each frame's start (q0, qdot,
+    Newton counter). Newton and line-search counts (the discrete decisions of the step)
+    must match on every frame."""
+    gpu = gpu or ABD(sc, cfg)
+    orc = O.OracleSim(sc, cfg, n_threads=os.cpu_count() or 1)
+    if start is not None:
+        orc.set_state(start[0], start[1])
+        orc.iter = start[2]
+    errs, starts = [], []
     for _ in range(frames):
         q0, qd = orc.state()
+        starts.append((q0, qd, orc.iter))
         gpu.set_state(q0, qd)
         gpu.iter = orc.iter
         sg = gpu.implicit_euler()
@@ -200,23 +235,108 @@ def run_pair(O, sc, cfg, frames):
         qo, vo = orc.state()
         errs.append(rel(qg, qo))
         assert gpu.iter == orc.iter
-    return np.array(errs)
+    return np.array(errs), starts
+
+
+def oracle_sensitivity(O, sc, cfg, start, n=4, eps=1e-16, seed=0):
+    """Largest relative change of the oracle's frame when its start positions are
+    perturbed by eps relative (n seeded perturbations): the reproducibility floor of the
+    reference step on that frame."""
+    q0, qd, it = start
+
+    def frame(q):
+        o = O.OracleSim(sc, cfg, n_threads=os.cpu_count() or 1)
+        o.set_state(q, qd)
+        o.iter = it
+        o.step(1)
+        return o.state()[0]
+
+    base = frame(q0)
+    rng = np.random.default_rng(seed)
+    return max(rel(frame(q0 * (1 + eps * rng.normal(size=q0.shape))), base) for _ in range(n))
+
+
+def assert_frames(O, sc, cfg, errs, starts):
+    """Every frame within REL, or, on a frame where the oracle's own sensitivity to
+    rounding-level perturbations is above REL / 10, within SENS_FACTOR of it."""
+    for k, e in enumerate(errs):
+        if e <= REL:
+            continue
+        s = oracle_sensitivity(O, sc, cfg, starts[k])
+        print("frame %d: GPU vs oracle %.2e, oracle sensitivity %.2e" % (k, e, s))
+        assert s > REL / 10 and e <= SENS_FACTOR * s, (k, e, s)
 
 
 def test_frames_match_oracle_cube_stack(O):
-    errs = run_pair(O, S.cube_stack(10, seed=0), S.workload_config("cubes"), 60)
+    errs, _ = run_pair(O, S.cube_stack(10, seed=0), S.workload_config("cubes"), 60)
     assert errs.max() <= REL
 
 
+def test_frames_match_oracle_cube_stack_500_frames(O):
+    """The 10-cube stack of the plain-method workload over all of its 500 frames."""
+    sc, cfg = S.cube_stack(10, seed=0), S.workload_config("cubes")
+    errs, starts = run_pair(O, sc, cfg, 500)
+    assert_frames(O, sc, cfg, errs, starts)
+
+
 def test_frames_match_oracle_small_pile(O):
-    # Frames whose line search cuts the step to alpha ~ 1e-3 for dozens of Newton
-    # iterations amplify the ~1e-12 difference between PCG and the direct solve; the
-    # bar is 1e-9 on 90% of the frames and 1e-7 on all.
-    errs = run_pair(O, S.sphere_pile(3, 3, 2, subdiv=1, seed=2), S.workload_config("pile"), 30)
-    assert np.quantile(errs, 0.9) <= REL and errs.max() <= 1e-7
+    sc, cfg = S.sphere_pile(3, 3, 2, subdiv=1, seed=2), S.workload_config("pile")
+    errs, starts = run_pair(O, sc, cfg, 30)
+    assert np.quantile(errs, 0.9) <= REL
+    assert_frames(O, sc, cfg, errs, starts)
 
 
 def test_frames_match_oracle_chain_with_static_link(O):
     cfg = S.workload_config("chain")
-    errs = run_pair(O, S.torus_chain(4, nu=16, nv=8, seed=3), cfg, 20)
-    assert np.quantile(errs, 0.9) <= REL and errs.max() <= 1e-7
+    sc = S.torus_chain(6, nu=24, nv=12, seed=3)
+    gpu = ABD(sc, cfg)
+    gpu.step(60)   # links swing into contact (first edge-edge pairs near frame 48)
+    q0, qd = gpu.state()
+    errs, starts = run_pair(O, sc, cfg, 30, start=(q0, qd, gpu.iter), gpu=gpu)
+    assert_frames(O, sc, cfg, errs, starts)
+
+
+def test_frames_match_oracle_full_chain(O):
+    """The 200-link chain of 48 x 24 tori at full size: the GPU steps it into contact,
+    then three frames are compared with the oracle from the same start states."""
+    sc, cfg = S.torus_chain(seed=0), S.workload_config("chain")
+    gpu = ABD(sc, cfg)
+    gpu.step(60)
+    q0, qd = gpu.state()
+    errs, starts = run_pair(O, sc, cfg, 3, start=(q0, qd, gpu.iter), gpu=gpu)
+    assert_frames(O, sc, cfg, errs, starts)
+
+
+PILE_CKPT = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "adb_gb300", "data",
+                         "pile_ckpt.npz")
+
+
+@pytest.fixture(scope="module")
+def full_pile(O):
+    z = np.load(PILE_CKPT)
+    return S.sphere_pile(seed=0), S.workload_config("pile"), z["q0"], z["qdot"]
+
+
+def test_cull_bit_exact_full_pile(O, full_pile):
+    """The 1024-icosphere pile at its contact-rich checkpoint: pair sets, types and order
+    at q (vtn 1) and at q + dq (vtn 2), and the trajectory TOI (vtn 3), all exact."""
+    sc, cfg, q0, qd = full_pile
+    gpu = ABD(sc, cfg)
+    orc = O.OracleSim(sc, cfg, n_threads=os.cpu_count() or 1)
+    g, o = gpu.cull(1, q0), orc.cull(1, q0)
+    assert len(o[0]) > 10000 and len(o[2]) > 10000
+    assert_sets_equal(g, o)
+    rng = np.random.default_rng(11)
+    dq = np.zeros_like(q0)
+    dq[:, :3] = rng.normal(size=(len(q0), 3)) * 2e-3
+    dq[:, 3:] = rng.normal(size=(len(q0), 9)) * 2e-4
+    assert_sets_equal(gpu.cull(2, q0, dq), orc.cull(2, q0, dq))
+    assert gpu.cull(3, q0, dq) == orc.cull(3, q0, dq)
+
+
+def test_frame_matches_oracle_full_pile(O, full_pile):
+    """One whole frame of the 1024-icosphere pile from its checkpoint."""
+    sc, cfg, q0, qd = full_pile
+    errs, starts = run_pair(O, sc, cfg, 1, start=(q0, qd, 0))
+    print("full pile frame: rel %.3e" % errs[0])
+    assert errs[0] <= REL

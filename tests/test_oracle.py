@@ -238,3 +238,20 @@ def test_oracle_cube_stack_runs(oracle_lib):
     # every body stays above the ground plane and the stack keeps its order
     assert np.all(q0[:, 1] > -0.5)
     assert np.all(np.diff(q0[:, 1]) > 0.9)
+
+
+def test_energy_terms_restate_the_line_search_energy(oracle_lib):
+    """orc_energy_terms at dq = 0: inertia + barrier terms add up to the line search's
+    E_barrier_plus_inert at q (orc_energy), and the per-pair values add up to the terms."""
+    O = oracle_lib
+    sc, cfg = S.cube_stack(4, gap=0.0005, seed=3), S.workload_config("cubes")
+    o = O.OracleSim(sc, cfg)
+    q = sc.q0.copy()
+    out = o.energy_terms(q, np.zeros_like(q))
+    t = out["terms"]
+    assert out["counts"][2] > 0 or out["counts"][0] > 0
+    assert abs(t[:4].sum() - o.energy(q)) <= 1e-12 * abs(t[:4].sum())
+    f = out["f_pt"].sum() + out["f_ee"].sum() + out["f_vg"].sum()
+    assert abs(f - t[4]) <= 1e-12 * max(abs(t[4]), 1e-300)
+    assert abs(out["e_pt"].sum() - t[1]) <= 1e-12 * max(abs(t[1]), 1e-300)
+    assert abs(out["e_vg"].sum() - t[3]) <= 1e-12 * max(abs(t[3]), 1e-300)
