@@ -29,7 +29,8 @@ class AbdConfig(C.Structure):
                 "safe_factor", "sh_min_xyz", "sh_dx")] + [(n, C.c_int) for n in (
                     "sh_xyz_bits", "sh_fix_edge_trajectory")] + [("dq_tol", C.c_double), ("damping", C.c_int),
                                                                  ("damp_alpha", C.c_double), ("damp_beta", C.c_double),
-                                                                 ("pcg_refine", C.c_int), ("pcg_refine_tol", C.c_double)]
+                                                                 ("pcg_refine", C.c_int), ("pcg_refine_tol", C.c_double),
+                                                                 ("solver", C.c_int)]
 
 
 class AbdSceneDesc(C.Structure):
@@ -66,6 +67,12 @@ def lib():
         L.abd_create_from_files.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(H)]
         L.abd_step.argtypes = [H, C.c_double, C.c_int, C.POINTER(AbdFrameStats)]
         L.abd_get_state.argtypes = [H, _D, _D]
+        L.abd_trace_save.argtypes = [H, C.c_char_p, C.c_int, C.c_int]
+        L.abd_trace_load.argtypes = [H, C.c_char_p, C.c_int]
+        L.abd_set_trace.argtypes = [H, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_char_p]
+        L.abd_get_trace.argtypes = [H, _I, _I, _I, C.c_char_p, C.c_int]
+        L.abd_trace_files.argtypes = [H, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p)]
+        L.abd_run.argtypes = [H, C.c_int, C.POINTER(AbdFrameStats)]
         L.abd_set_state.argtypes = [H, _D, _D]
         L.abd_get_counts.argtypes = [H, _I, _I, _I, _I]
         L.abd_get_iter.argtypes = [H]
@@ -103,7 +110,7 @@ def lib():
 
 
 # Every symbol include/abd_gb300.h declares (checked by the CPU test suite).
-EXPORTED = ["abd_create", "abd_create_from_files", "abd_step", "abd_get_state", "abd_set_state", "abd_get_counts",
+EXPORTED = ["abd_create", "abd_create_from_files", "abd_step", "abd_get_state", "abd_set_state", "abd_trace_save", "abd_trace_load", "abd_set_trace", "abd_get_trace", "abd_trace_files", "abd_run", "abd_get_counts",
             "abd_get_iter", "abd_set_iter", "abd_get_scene_count", "abd_get_scene_stats", "abd_set_friction", "abd_get_friction", "abd_adjoint_frame", "abd_last_error", "abd_destroy", "abd_profile", "abd_kernel_times", "abd_kernel_work", "abd_cull", "abd_get_pairs",
             "abd_newton_system", "abd_newton_dq", "abd_energy", "abd_ipc_hess_pt_batch", "abd_ipc_hess_ee_batch",
             "abd_pt_collision_time_batch", "abd_ee_collision_time_batch", "abd_pt_distance_batch",

@@ -32,6 +32,9 @@ def make_abd_config(cfg: Config) -> L.AbdConfig:
     c.sh_fix_edge_trajectory, c.dq_tol = int(cfg.sh_fix_edge_trajectory), cfg.dq_tol
     c.damping, c.damp_alpha, c.damp_beta = int(cfg.damping), cfg.damp_alpha, cfg.damp_beta
     c.pcg_refine, c.pcg_refine_tol = int(cfg.pcg_refine), cfg.pcg_refine_tol
+    if cfg.solver not in ("sparse", "dense"):
+        raise ValueError('solver must be "sparse" or "dense"')
+    c.solver = 1 if cfg.solver == "dense" else 0
     return c
 
 
@@ -107,6 +110,37 @@ class ABD:
         qd = None if qdot is None else np.ascontiguousarray(qdot, np.float64)
         L.check(L.lib().abd_set_state(self._h, L.dptr(q0), None if qd is None else L.dptr(qd)), self._h,
                 "abd_set_state")
+
+    # --- traces and the viewer loop (C++ front end) -------------------------------------
+    def trace_save(self, folder: str, ts: int, init: bool = False):
+        """Writes the state as frame file <folder>/<ts> (the reference's player_save)."""
+        L.check(L.lib().abd_trace_save(self._h, folder.encode(), int(ts), int(init)), self._h, "abd_trace_save")
+
+    def trace_load(self, folder: str, ts: int):
+        """Loads frame file <folder>/<ts> into the state (the reference's player_load)."""
+        L.check(L.lib().abd_trace_load(self._h, folder.encode(), int(ts)), self._h, "abd_trace_load")
+
+    def set_trace(self, folder: Optional[str] = None, ts: int = 0, starting_ts: int = -1, ending_ts: int = 0):
+        L.check(L.lib().abd_set_trace(self._h, folder.encode() if folder else None, int(ts), int(starting_ts),
+                                      int(ending_ts), None, None), self._h, "abd_set_trace")
+
+    @property
+    def trace(self) -> dict:
+        """Trace settings: folder, frame counter ts, starting_ts, ending_ts."""
+        ts, st, en = C.c_int(), C.c_int(), C.c_int()
+        buf = C.create_string_buffer(4096)
+        L.check(L.lib().abd_get_trace(self._h, C.byref(ts), C.byref(st), C.byref(en), buf, 4096), self._h,
+                "abd_get_trace")
+        return {"folder": buf.value.decode(), "ts": ts.value, "starting_ts": st.value, "ending_ts": en.value}
+
+    def run(self, record: bool = False) -> L.AbdFrameStats:
+        """The reference's viewer loop without rendering: frames until ts reaches ending_ts,
+        each new state saved as a frame file when recording."""
+        st = L.AbdFrameStats()
+        rc = L.lib().abd_run(self._h, int(record), C.byref(st))
+        if rc not in (0, 6):
+            L.check(rc, self._h, "abd_run")
+        return st
 
     @property
     def iter(self) -> int:

@@ -238,6 +238,8 @@ struct NewtonBufs {
   DBuf<int> rcol, rn;
   DBuf<double> gpA, gpB;     // per-group partial sums of the PCG
   DBuf<int> grp_body, grp_n, grp_scene, sc_gbeg, sc_gend;  // PCG body groups (pcg_groups)
+  std::vector<int> h_sc_beg, h_sc_end;  // body range of each scene (host)
+  DBuf<double> dense_A, dense_y;         // dense solve: one scene's matrix and right-hand side
   int ngrp = 0;
   DBuf<double> sc_rz, sc_bb; // per-scene CG scalars
   DBuf<int> sc_conv, sc_iters, n_active;
@@ -257,10 +259,22 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& nb, cudaStr
 // Body groups of the PCG (consecutive bodies of one scene, cut from the scene's first
 // body); called once per handle with the scenes' body ranges.
 void pcg_groups(const std::vector<int>& sc_beg, const std::vector<int>& sc_end, NewtonBufs& nb, cudaStream_t s);
-// refine > 0: that many iterative-refinement passes, each solving H d = b - H x (true
-// residual) by the same PCG to refine_tol relative and adding d to x.
-int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& nb, double rel_tol, int max_iter, const int* sc_on, double* dq,
-              cudaStream_t s, int* status, int* scene_iters, int refine = 0, double refine_tol = 1e-8);
+// Newton-solve controls: PCG relative residual and iteration cap; refine > 0: that many
+// iterative-refinement passes, each solving H d = b - H x (true residual) by the same PCG
+// to refine_tol relative and adding d to x; dense: a dense Cholesky per scene instead of
+// the PCG (the reference's "solver": "dense").
+struct SolveOpts {
+  double rel_tol = 1e-14;
+  int max_iter = 5000;
+  int refine = 0;
+  double refine_tol = 1e-8;
+  int dense = 0;
+};
+// on (host, ns): the scenes solved (the others get dq = 0); sc_on is its device copy.
+int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& nb, const SolveOpts& o, const int* sc_on,
+              const std::vector<char>& on, double* dq, cudaStream_t s, int* status, int* scene_iters);
+// Dense Cholesky solve of each scene's system (after the row-block copy of pcg_solve).
+void dense_solve(const Geo& g, PairSet& S, NewtonBufs& B, const std::vector<char>& on, double* dq, cudaStream_t s);
 // Line-search energy of every scene at the trial configuration (X must hold q + alpha dq):
 // inertia + barrier over `Snew` + lagged friction over `Slag`; out (host) receives ns values.
 void energy(const Geo& g, const Params& P, double alpha, PairSet& Snew, PairSet& Slag, bool with_barrier_inertia,

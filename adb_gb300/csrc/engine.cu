@@ -105,6 +105,11 @@ struct Engine {
   double *h_alpha = nullptr, *h_factor = nullptr;
   std::string err;
   Prof prof;
+  // trace settings of the reference's viewer loop (view/control.cpp:41,84-90;
+  // view/model_view.cpp:282-295): frame counter, last frame, folder, and the config and
+  // scene files copied into a new trace folder
+  int ts = 0, starting_ts = -1, ending_ts = 0;
+  std::string trace_folder = "trace", trace_config, trace_scene;
 
   Geo geo() const {
     Geo g;
@@ -157,6 +162,7 @@ struct Engine {
     nbufs.e_off.release(); nbufs.e_chunk_cnt.release(); nbufs.e_chunk_off.release(); nbufs.e_scan_tmp.release();
     nbufs.e_out.release(); nbufs.red.release(); nbufs.status.release();
     nbufs.xr.release(); nbufs.rt.release(); nbufs.dqc.release(); nbufs.it_ref.release();
+    nbufs.dense_A.release(); nbufs.dense_y.release();
     if (nbufs.h_red) cudaFreeHost(nbufs.h_red);
     if (nbufs.h_int) cudaFreeHost(nbufs.h_int);
     if (h_on) cudaFreeHost(h_on);
@@ -343,6 +349,16 @@ struct Engine {
     else sh_cull(g, P, sh, vtn, alpha, shw, cs, S, s);
   }
 
+  SolveOpts solve_opts() const {
+    SolveOpts o;
+    o.rel_tol = cfg.pcg_rel_tol;
+    o.max_iter = cfg.pcg_max_iter;
+    o.refine = cfg.pcg_refine;
+    o.refine_tol = cfg.pcg_refine_tol;
+    o.dense = cfg.solver == 1;
+    return o;
+  }
+
   // Uploads of per-scene values go through pinned staging arrays; every upload is followed
   // by a stream synchronisation before its staging array is written again.
   void put_on(const std::vector<char>& on) {
@@ -400,11 +416,11 @@ struct Engine {
       st.bytes_moved += bytes_assemble(S);
       auto t1 = clk::now();
       int pst = 0;
-      int its = pcg_solve(g, S, nbufs, cfg.pcg_rel_tol, cfg.pcg_max_iter, sc_on.p, dq.p, s, &pst, its_s.data(),
-                          cfg.pcg_refine, cfg.pcg_refine_tol);
+      int its = pcg_solve(g, S, nbufs, solve_opts(), sc_on.p, act, dq.p, s, &pst, its_s.data());
       st.pcg_iters += its;
       for (int k = 0; k < ns; ++k) sc_pcg[k] += its_s[k];
-      st.bytes_moved += its * (1152.0 * (nb + 2.0 * S.nov) + 6 * 96.0 * nb) + 1152.0 * nb;
+      // N_blk = bodies + 2 x contacting body pairs: the blocks the PCG keeps (nbufs.h_int[2])
+      st.bytes_moved += its * (1152.0 * nbufs.h_int[2] + 6 * 96.0 * nb) + 1152.0 * nb;
       if (pst == ABD_ERR_NOT_SPD) return ABD_ERR_NOT_SPD;
       if (pst == ABD_ERR_PCG_NOCONV) status = ABD_ERR_PCG_NOCONV;
       dots(g, dq.p, nbufs.grad.p, nbufs, dd.data(), s);
@@ -922,6 +938,40 @@ int abd_set_friction(abd_handle* h, double mu) {
   return ABD_OK;
 }
 
+int abd_set_trace(abd_handle* h, const char* folder, int ts, int starting_ts, int ending_ts, const char* config_json,
+                  const char* scene_json) {
+  if (!h || ts < 0) return ABD_ERR_INVALID;
+  Engine& e = h->e;
+  if (folder) e.trace_folder = folder;
+  e.ts = ts;
+  e.starting_ts = starting_ts;
+  e.ending_ts = ending_ts;
+  if (config_json) e.trace_config = config_json;
+  if (scene_json) e.trace_scene = scene_json;
+  return ABD_OK;
+}
+
+int abd_get_trace(abd_handle* h, int* ts, int* starting_ts, int* ending_ts, char* folder, int folder_cap) {
+  if (!h) return ABD_ERR_INVALID;
+  Engine& e = h->e;
+  if (ts) *ts = e.ts;
+  if (starting_ts) *starting_ts = e.starting_ts;
+  if (ending_ts) *ending_ts = e.ending_ts;
+  if (folder && folder_cap > 0) {
+    std::strncpy(folder, e.trace_folder.c_str(), folder_cap - 1);
+    folder[folder_cap - 1] = 0;
+  }
+  if (folder && folder_cap > 0 && (int)e.trace_folder.size() >= folder_cap) return ABD_ERR_INVALID;
+  return ABD_OK;
+}
+
+int abd_trace_files(abd_handle* h, const char** config_json, const char** scene_json) {
+  if (!h) return ABD_ERR_INVALID;
+  if (config_json) *config_json = h->e.trace_config.empty() ? nullptr : h->e.trace_config.c_str();
+  if (scene_json) *scene_json = h->e.trace_scene.empty() ? nullptr : h->e.trace_scene.c_str();
+  return ABD_OK;
+}
+
 int abd_get_friction(abd_handle* h, double* mu) {
   if (!h || !mu) return ABD_ERR_INVALID;
   *mu = h->e.P.mu;
@@ -966,8 +1016,8 @@ int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const
     for (int it = 0; it < 50; ++it) {
       for (size_t k = 0; k < n; ++k) rhs[k] = gq_next[k] - ctw[k];
       CK(cudaMemcpyAsync(e.nbufs.grad.p, rhs.data(), n * sizeof(double), cudaMemcpyHostToDevice, e.s));
-      abd::pcg_solve(g, S, e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.sc_on.p, e.dq.p, e.s, &st, nullptr,
-                     e.cfg.pcg_refine, e.cfg.pcg_refine_tol);
+      abd::pcg_solve(g, S, e.nbufs, e.solve_opts(), e.sc_on.p, std::vector<char>(e.ns, 1), e.dq.p, e.s, &st,
+                     nullptr);
       if (st == ABD_ERR_NOT_SPD) return st;
       wprev = w;
       CK(cudaMemcpyAsync(w.data(), e.nbufs.x.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
@@ -1020,8 +1070,8 @@ int abd_newton_dq(abd_handle* h, const double* q, double* dq, int* pcg_iters) {
     newton_system_at(e, q);
     int st = 0;
     e.put_on(std::vector<char>(e.ns, 1));
-    int its = abd::pcg_solve(e.geo(), e.sets[e.cur], e.nbufs, e.cfg.pcg_rel_tol, e.cfg.pcg_max_iter, e.sc_on.p,
-                             e.dq.p, e.s, &st, nullptr, e.cfg.pcg_refine, e.cfg.pcg_refine_tol);
+    int its = abd::pcg_solve(e.geo(), e.sets[e.cur], e.nbufs, e.solve_opts(), e.sc_on.p, std::vector<char>(e.ns, 1),
+                             e.dq.p, e.s, &st, nullptr);
     if (pcg_iters) *pcg_iters = its;
     CK(cudaMemcpy(dq, e.dq.p, 12 * (size_t)e.nb * sizeof(double), cudaMemcpyDeviceToHost));
     return st;

@@ -2,9 +2,11 @@
 // (view/control.cpp:19-111) and scene JSON (test_cases/spinning_cube.cpp:56-127) with a
 // small JSON reader, loads Wavefront OBJ meshes (the reference loads them through
 // assimp, view/model.h) and builds the scene descriptor for abd_create.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <map>
 #include <memory>
@@ -195,6 +197,17 @@ Mesh cube_mesh() {
   return m;
 }
 
+// Frame file <folder>/<ts> of a trace: 24 doubles per body (player_load, mutils.cpp:257-276).
+int read_trace_frame(const std::string& folder, int ts, std::vector<double>& buf) {
+  std::ifstream in(folder + "/" + std::to_string(ts), std::ios::binary | std::ios::ate);
+  if (!in) return ABD_ERR_IO;
+  std::streamsize n = in.tellg();
+  if (n != (std::streamsize)(buf.size() * sizeof(double))) return ABD_ERR_IO;
+  in.seekg(0);
+  in.read(reinterpret_cast<char*>(buf.data()), n);
+  return in ? ABD_OK : ABD_ERR_IO;
+}
+
 // geometry.cpp:248-264: Rz(a) Ry(b) Rx(c)
 void rotation(double a, double b, double c, double R[3][3]) {
   double s1 = std::sin(a), s2 = std::sin(b), s3 = std::sin(c);
@@ -245,6 +258,8 @@ extern "C" int abd_create_from_files(const char* config_json, const char* scene_
   c.pcg_max_iter = (int)cfgj.num("pcg_max_iter", 5000);
   c.pcg_refine = (int)cfgj.num("pcg_refine", 0);
   c.pcg_refine_tol = cfgj.num("pcg_refine_tol", 1e-8);
+  const JV* sv = cfgj.get("solver");
+  c.solver = (sv && sv->t == JV::STR && sv->s == "dense") ? 1 : 0;
   c.iaabb = (int)cfgj.num("iaabb", 3);
   c.full_ccd = cfgj.flag("full_ccd", true);
   c.safe_factor = cfgj.num("safe_factor", 1.0);
@@ -334,5 +349,129 @@ extern "C" int abd_create_from_files(const char* config_json, const char* scene_
   d.face_off = fo.data();
   d.faces = faces.data();
   d.scene_id = nullptr;
-  return abd_create(&d, &c, out);
+  // trace settings (view/control.cpp:41, 84-90): a non-negative starting_ts resumes from
+  // frame file <trace_folder>/<starting_ts> of a reference trace
+  const JV* tf = cfgj.get("trace_folder");
+  std::string folder = (tf && tf->t == JV::STR) ? tf->s : std::string("trace");
+  int starting_ts = (int)cfgj.num("starting_ts", -1);
+  int ending_ts = (int)cfgj.num("ending_ts", 0);
+  if (starting_ts >= 0) {
+    std::vector<double> buf(24 * (size_t)d.n_bodies);
+    if (read_trace_frame(folder, starting_ts, buf) != ABD_OK) return ABD_ERR_IO;
+    for (int b = 0; b < d.n_bodies; ++b)
+      for (int k = 0; k < 12; ++k) {
+        q0[12 * (size_t)b + k] = buf[24 * (size_t)b + k];
+        qd[12 * (size_t)b + k] = buf[24 * (size_t)b + 12 + k];
+      }
+  }
+  int rc = abd_create(&d, &c, out);
+  if (rc != ABD_OK) return rc;
+  abd_set_trace(*out, folder.c_str(), starting_ts >= 0 ? starting_ts : 0, starting_ts, ending_ts, config_json,
+                scene_json);
+  return ABD_OK;
+}
+
+// ---- traces in the reference's binary layout (player_save / player_load,
+//      model/mutils.cpp:257-276, 293-329): one file per frame, <folder>/<ts>, holding per
+//      body q0 (p, a1, a2, a3) then dqdt as raw doubles ----
+
+extern "C" int abd_trace_save(abd_handle* h, const char* folder, int ts, int init) {
+  if (!h || !folder || ts < 0) return ABD_ERR_INVALID;
+  int nb = 0;
+  abd_get_counts(h, &nb, nullptr, nullptr, nullptr);
+  std::vector<double> q0(12 * (size_t)nb), qd(12 * (size_t)nb), buf(24 * (size_t)nb);
+  int rc = abd_get_state(h, q0.data(), qd.data());
+  if (rc != ABD_OK) return rc;
+  namespace fs = std::filesystem;
+  std::error_code ec;
+  if (init) {  // a new trace: the folder is recreated and the run's config and scene copied in
+    fs::remove_all(folder, ec);
+    fs::create_directories(folder, ec);
+    if (ec) return ABD_ERR_IO;
+    const char *cj = nullptr, *sj = nullptr;
+    abd_trace_files(h, &cj, &sj);
+    for (const char* f : {cj, sj})
+      if (f) {
+        fs::copy_file(f, fs::path(folder) / fs::path(f).filename(), fs::copy_options::overwrite_existing, ec);
+        if (ec) return ABD_ERR_IO;
+      }
+  } else {
+    fs::create_directories(folder, ec);
+  }
+  for (int b = 0; b < nb; ++b)
+    for (int k = 0; k < 12; ++k) {
+      buf[24 * (size_t)b + k] = q0[12 * (size_t)b + k];
+      buf[24 * (size_t)b + 12 + k] = qd[12 * (size_t)b + k];
+    }
+  std::ofstream out(std::string(folder) + "/" + std::to_string(ts), std::ios::binary | std::ios::trunc);
+  if (!out) return ABD_ERR_IO;
+  out.write(reinterpret_cast<const char*>(buf.data()), buf.size() * sizeof(double));
+  return out ? ABD_OK : ABD_ERR_IO;
+}
+
+extern "C" int abd_trace_load(abd_handle* h, const char* folder, int ts) {
+  if (!h || !folder || ts < 0) return ABD_ERR_INVALID;
+  int nb = 0;
+  abd_get_counts(h, &nb, nullptr, nullptr, nullptr);
+  std::vector<double> buf(24 * (size_t)nb), q0(12 * (size_t)nb), qd(12 * (size_t)nb);
+  int rc = read_trace_frame(folder, ts, buf);
+  if (rc != ABD_OK) return rc;
+  for (int b = 0; b < nb; ++b)
+    for (int k = 0; k < 12; ++k) {
+      q0[12 * (size_t)b + k] = buf[24 * (size_t)b + k];
+      qd[12 * (size_t)b + k] = buf[24 * (size_t)b + 12 + k];
+    }
+  return abd_set_state(h, q0.data(), qd.data());
+}
+
+// The reference's viewer loop without its rendering (view/model_view.cpp:282-295): one
+// frame per pass; the frame counter advances inside the step (abd.cpp:116) and, when
+// recording, the new state is written as frame file <folder>/<ts> (the folder is
+// recreated on the pass that starts at ts 0); stops once ts reaches ending_ts.
+extern "C" int abd_run(abd_handle* h, int record, abd_frame_stats* stats) {
+  if (!h) return ABD_ERR_INVALID;
+  int ts = 0, st0 = 0, end = 0;
+  char folder[4096];
+  if (abd_get_trace(h, &ts, &st0, &end, folder, sizeof(folder)) != ABD_OK) return ABD_ERR_INVALID;
+  if (end <= 0) return ABD_ERR_INVALID;  // no last frame: the loop would not end
+  abd_frame_stats total;
+  std::memset(&total, 0, sizeof(total));
+  total.toi_min = 1.0;
+  total.alpha_min = 1.0;
+  int rc = ABD_OK;
+  while (ts < end) {
+    bool init = ts == 0;
+    abd_frame_stats f;
+    rc = abd_step(h, 0.0, 1, &f);
+    ++ts;
+    abd_set_trace(h, nullptr, ts, st0, end, nullptr, nullptr);
+    total.frames += f.frames;
+    total.newton_iters += f.newton_iters;
+    total.ls_trials += f.ls_trials;
+    total.pcg_iters += f.pcg_iters;
+    total.n_pt = std::max(total.n_pt, f.n_pt);
+    total.n_ee = std::max(total.n_ee, f.n_ee);
+    total.n_vg = std::max(total.n_vg, f.n_vg);
+    total.n_overlaps = std::max(total.n_overlaps, f.n_overlaps);
+    total.kernel_launches += f.kernel_launches;
+    total.toi_min = std::min(total.toi_min, f.toi_min);
+    total.alpha_min = std::min(total.alpha_min, f.alpha_min);
+    total.t_ipc_ms += f.t_ipc_ms;
+    total.t_solver_ms += f.t_solver_ms;
+    total.t_ccd_ms += f.t_ccd_ms;
+    total.t_ls_ms += f.t_ls_ms;
+    total.bytes_moved += f.bytes_moved;
+    total.device_ms += f.device_ms;
+    total.status = rc;
+    if (rc != ABD_OK && rc != ABD_ERR_PCG_NOCONV && rc != ABD_ERR_LS_STALL) break;
+    if (record) {
+      int wr = abd_trace_save(h, folder, ts, init ? 1 : 0);
+      if (wr != ABD_OK) {
+        rc = wr;
+        break;
+      }
+    }
+  }
+  if (stats) *stats = total;
+  return rc;
 }

@@ -1978,8 +1978,10 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
                                    S.vg_lam.p, B.D.p, B.grad.p));
 }
 
-int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_iter, const int* sc_on, double* dq,
-              cudaStream_t s, int* status, int* scene_iters, int refine, double refine_tol) {
+int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, const SolveOpts& o, const int* sc_on,
+              const std::vector<char>& on, double* dq, cudaStream_t s, int* status, int* scene_iters) {
+  const double rel_tol = o.rel_tol, refine_tol = o.refine_tol;
+  const int max_iter = o.max_iter, refine = o.refine;
   int nb = g.nb, ns = g.ns;
   B.status.ensure(4);
   if (!B.h_int) CK(cudaMallocHost(&B.h_int, 16 * sizeof(int)));
@@ -2010,6 +2012,16 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, double rel_tol, int max_i
                                                                                         S.upidx.p, B.has.p, B.ovr.p,
                                                                                         B.D.p, B.Hrow.p, B.rcol.p,
                                                                                         B.rn.p, B.status.p + 2));
+  if (o.dense) {
+    dense_solve(g, S, B, on, dq, s);
+    CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *status = B.h_int[0];
+    if (scene_iters)
+      for (int k = 0; k < ns; ++k) scene_iters[k] = 0;
+    prof_work(K_BLOCK_INVERSE, 1, 2 * 1152.0 * B.h_int[2]);
+    return 0;
+  }
   static int max_blocks = 0, max_blocks1 = 0;
   if (!max_blocks) {
     int dev, sms, per, per1;
@@ -2118,6 +2130,8 @@ void pcg_groups(const std::vector<int>& sc_beg, const std::vector<int>& sc_end, 
     sge.push_back((int)gb.size());
   }
   B.ngrp = (int)gb.size();
+  B.h_sc_beg = sc_beg;
+  B.h_sc_end = sc_end;
   DBuf<int>* dst[] = {&B.grp_body, &B.grp_n, &B.grp_scene, &B.sc_gbeg, &B.sc_gend};
   std::vector<int>* src[] = {&gb, &gn, &gs, &sgb, &sge};
   for (int i = 0; i < 5; ++i) {

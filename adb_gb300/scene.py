@@ -68,7 +68,7 @@ class Config:
     damping: bool = False          # "damping": {"enable", "alpha", "beta"} (mutils.cpp:106-115)
     damp_alpha: float = 5e-2
     damp_beta: float = 2.5e-2
-    solver: str = "sparse"         # "solver": the reference's factorization choice; one PCG here
+    solver: str = "sparse"         # "solver": "sparse" (block-Jacobi PCG) or "dense" (per-scene dense Cholesky)
     # GPU solver controls (no reference counterpart: the reference factorizes directly)
     pcg_rel_tol: float = 1e-14
     pcg_max_iter: int = 5000

@@ -77,6 +77,10 @@ typedef struct {
    * error of a direct solve. */
   int pcg_refine;
   double pcg_refine_tol;
+  /* "solver" (view/control.cpp:29-30): 0 "sparse" (block-Jacobi PCG over the block-sparse
+   * system), 1 "dense" (the scene's full 12 n x 12 n matrix factorized by a dense Cholesky,
+   * as the reference's big_hess.ldlt(), abd.cpp:233-264; for small scenes) */
+  int solver;
 } abd_config;
 
 /* Scene: bodies with their rest meshes (local vertex ids per body). */
@@ -121,6 +125,26 @@ int abd_create_from_files(const char* config_json, const char* scene_json, abd_h
 /* Replaces ABD::implicit_euler(dt) (model/abd.cpp:30): advances n_frames frames. */
 int abd_step(abd_handle* h, double dt, int n_frames, abd_frame_stats* stats);
 int abd_get_state(abd_handle* h, double* q0, double* qdot);
+/* ---- traces and the viewer loop (view/control.cpp:41,84-90; view/model_view.cpp:282-295) ----
+ * Frame files in the reference's binary layout (player_save / player_load,
+ * model/mutils.cpp:257-276, 293-329): <folder>/<ts> holds, per body, q0 (p, a1, a2, a3)
+ * then dqdt, as raw doubles. abd_create_from_files reads "trace_folder", "starting_ts"
+ * (>= 0: the initial state is loaded from that frame file and the frame counter starts
+ * there) and "ending_ts" of the config. */
+int abd_trace_save(abd_handle* h, const char* folder, int ts, int init); /* init: recreate the folder,
+                                                                            copy config and scene in */
+int abd_trace_load(abd_handle* h, const char* folder, int ts);
+/* Trace settings of the handle: folder, frame counter ts, starting_ts, ending_ts, and the
+ * config / scene files a new trace folder receives (either may be NULL). */
+int abd_set_trace(abd_handle* h, const char* folder, int ts, int starting_ts, int ending_ts, const char* config_json,
+                  const char* scene_json);
+int abd_get_trace(abd_handle* h, int* ts, int* starting_ts, int* ending_ts, char* folder, int folder_cap);
+int abd_trace_files(abd_handle* h, const char** config_json, const char** scene_json);
+/* The viewer loop without rendering: steps frame after frame until the frame counter
+ * reaches ending_ts; with record != 0 each new state is saved as frame file <ts> (the
+ * folder recreated on the pass that starts at ts 0, as the reference does). stats sums
+ * the frames. */
+int abd_run(abd_handle* h, int record, abd_frame_stats* stats);
 int abd_set_state(abd_handle* h, const double* q0, const double* qdot);
 int abd_get_counts(abd_handle* h, int* n_bodies, int* n_vertices, int* n_edges, int* n_faces);
 /* Cumulative Newton counter (the reference's ABD::iter, model/abd.h:53); of scene 0 for
