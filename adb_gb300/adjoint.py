@@ -3,19 +3,18 @@
 ``rollout(sim, q0, v0, mu, n_steps, every)`` advances ``n_steps`` frames with
 ``ABD.implicit_euler`` and returns the final ``(q, v)``; gradients with respect to the
 initial state, the initial velocities and the friction coefficient come from the adjoint
-of each converged frame (``abd_adjoint_frame``: implicit differentiation, solved by the
-same block-sparse PCG). Forward states are kept every ``every`` frames (every frame by
+of each converged frame (``abd_adjoint_frame``: implicit differentiation on the GPU). Forward states are kept every ``every`` frames (every frame by
 default: a state is 24 doubles per body); the backward pass recomputes the frames between
 checkpoints from the one before them and walks each segment in reverse. The frame's velocity
 update v_{t+1} = (q_{t+1} - q_t) / dt (model/abd.cpp:128-139) is differentiated here.
 
-The adjoint system uses the exact Hessian (no PSD projection, the ground barrier's full
-second derivative) and the coupling through the ground-friction multipliers, which follow
-the vertex heights at the solution; with those, gradients match central differences of
-the reference step to the finite differences' resolution. The multipliers and tangent
-bases of point-triangle and edge-edge friction are held fixed (the Newton iteration holds
-them fixed within a frame), so where friction between bodies matters the gradient is
-that of the lagged scheme and can differ from finite differences of the converged map.
+The adjoint system uses the exact Jacobian of the frame's optimality condition at its
+solution: the Hessian without PSD projection (the ground barrier's full second
+derivative), plus the dependence of every friction multiplier and tangent frame on the
+configuration (ground, point-triangle and edge-edge; the reference recomputes them at
+every Newton iterate, so the converged state carries them at its own positions). It is
+solved by GMRES preconditioned with the forward step's Newton matrix. Gradients match
+central differences of the reference step to the finite differences' resolution.
 """
 from __future__ import annotations
 

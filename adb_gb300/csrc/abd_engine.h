@@ -240,6 +240,11 @@ struct NewtonBufs {
   DBuf<int> grp_body, grp_n, grp_scene, sc_gbeg, sc_gend;  // PCG body groups (pcg_groups)
   std::vector<int> h_sc_beg, h_sc_end;  // body range of each scene (host)
   DBuf<double> dense_A, dense_y;         // dense solve: one scene's matrix and right-hand side
+  // adjoint: friction-frame Jacobians and contributions per pair, the exact system's
+  // blocks, GMRES bases
+  DBuf<double> fj_pt, fj_ee, fc_pt, fc_ee, D_ex, ovr_ex, adj_V, adj_Z, adj_w, adj_t, adj_x;
+  DBuf<int> has_ex;
+  double* h_dot = nullptr;               // pinned: one dot product
   int ngrp = 0;
   DBuf<double> sc_rz, sc_bb; // per-scene CG scalars
   DBuf<int> sc_conv, sc_iters, n_active;
@@ -292,6 +297,18 @@ void launch_copy_scene(const Geo& g, double* dst, const double* src, const int* 
 void launch_scale_scene(const Geo& g, double* v, const double* f, cudaStream_t st);
 // y = H x with the system assembled last on S (no synchronisation)
 void spmv(const Geo& g, const PairSet& S, NewtonBufs& nb, const double* x, double* y, cudaStream_t st);
+// y = H x with explicitly given blocks (saved copies of an assembly on S)
+void spmv_blocks(const Geo& g, const PairSet& S, const int* has, const double* ovr, const double* D, const double* x,
+                 double* y, cudaStream_t st);
+// ---------------- adjoint (adjoint.cu) ----------------
+// Per PT/EE pair of S: the Jacobian of its friction force through its tangent frame and
+// multiplier at the positions in g.X (reference positions g.X0), kept in B.fj_pt / fj_ee.
+void fric_frame_jacobians(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStream_t s);
+// out = (those Jacobians, in body coordinates)^T w, summed per body in a fixed order
+// (needs the overlap segments of the last assembly on S).
+void fric_frame_apply_t(const Geo& g, PairSet& S, NewtonBufs& B, const double* w, double* out, cudaStream_t s);
+double dev_dot(int n, const double* a, const double* b, NewtonBufs& B, cudaStream_t s);  // synchronises
+void dev_axpby(int n, double a, const double* x, double b, double* y, cudaStream_t s);   // y = a x + b y
 // out = C^T w for the ground-friction multiplier coupling of an adjoint system
 void vg_lag_adjoint(const Geo& g, const Params& P, const PairSet& S, const double* w, double* out, cudaStream_t st);
 void launch_q_update_scene(const Geo& g, double* q, const double* dq, const double* alpha, cudaStream_t st);

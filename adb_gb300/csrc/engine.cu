@@ -163,6 +163,10 @@ struct Engine {
     nbufs.e_out.release(); nbufs.red.release(); nbufs.status.release();
     nbufs.xr.release(); nbufs.rt.release(); nbufs.dqc.release(); nbufs.it_ref.release();
     nbufs.dense_A.release(); nbufs.dense_y.release();
+    nbufs.fj_pt.release(); nbufs.fj_ee.release(); nbufs.fc_pt.release(); nbufs.fc_ee.release();
+    nbufs.D_ex.release(); nbufs.ovr_ex.release(); nbufs.has_ex.release(); nbufs.adj_V.release();
+    nbufs.adj_Z.release(); nbufs.adj_w.release(); nbufs.adj_t.release(); nbufs.adj_x.release();
+    if (nbufs.h_dot) cudaFreeHost(nbufs.h_dot);
     if (nbufs.h_red) cudaFreeHost(nbufs.h_red);
     if (nbufs.h_int) cudaFreeHost(nbufs.h_int);
     if (h_on) cudaFreeHost(h_on);
@@ -981,69 +985,176 @@ int abd_get_friction(abd_handle* h, double* mu) {
 // Adjoint of one converged frame by implicit differentiation. At the frame's solution
 // q_{t+1} the gradient r(q; q_t, v_t, mu) of the incremental potential vanishes, so
 // dL/dtheta = -w^T dr/dtheta with J^T w = dL/dq_{t+1}, J the Jacobian of r at q_{t+1}:
-// the exact Hessian (no PSD projection, no damping, the ground barrier's full second
-// derivative) plus the coupling through the ground-friction multipliers, which follow the
-// vertex heights at the solution (folded in by a fixed-point iteration around the PCG).
+//   J = H + C + F,
+// H the exact Hessian (no PSD projection, no damping, the ground barrier's full second
+// derivative, the friction Hessian with every tangent frame and multiplier held), C the
+// coupling through the ground-friction multipliers (which follow the vertex heights), F
+// the point-triangle / edge-edge friction forces' Jacobian through their tangent frames,
+// closest points and multipliers (all recomputed at every Newton iterate by the reference,
+// pt_ipc.cpp:22-107, ee_ipc.cpp:21-118). J is not symmetric (the friction force is not a
+// potential's gradient once its frame moves) and H can be indefinite, so J^T w = g is
+// solved by flexible GMRES preconditioned with the Newton matrix of the forward step at
+// q_{t+1} (PSD-projected, SPD), applied by the block-Jacobi PCG. Then
 // dr/dq_t = -M - mu K (inertia through q_tilde, friction through the reference positions
-// x(q_t)), dr/dv_t = -dt M, dr/dmu = r_friction / mu, with K and r_friction assembled at
-// mu = 1. Point-triangle and edge-edge friction multipliers and tangent bases are held
-// fixed, as the forward Newton iteration holds them.
+// x(q_t), K the friction Hessian with frames held), dr/dv_t = -dt M, dr/dmu =
+// r_friction / mu; K and r_friction are assembled at mu = 1.
 int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const double* q_next,
                       const double* gq_next, double* gq_t, double* gv_t, double* gmu) {
   if (!h || !q_t || !v_t || !q_next || !gq_next || !gq_t || !gv_t) return ABD_ERR_INVALID;
   return guarded(h, [&]() {
     Engine& e = h->e;
     const int nb = e.nb;
-    size_t n = 12 * (size_t)nb;
-    CK(cudaMemcpyAsync(e.q0.p, q_t, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
-    CK(cudaMemcpyAsync(e.dqdt.p, v_t, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
-    CK(cudaMemcpyAsync(e.q.p, q_next, n * sizeof(double), cudaMemcpyHostToDevice, e.s));
-    CK(cudaMemsetAsync(e.dq.p, 0, n * sizeof(double), e.s));
+    const int n = 12 * nb;
+    abd::NewtonBufs& B = e.nbufs;
+    cudaStream_t s = e.s;
+    CK(cudaMemcpyAsync(e.q0.p, q_t, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(e.dqdt.p, v_t, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(e.q.p, q_next, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(e.dq.p, 0, n * sizeof(double), s));
     abd::Geo g = e.geo();
     abd::PairSet& S = e.sets[e.cur];
-    abd::launch_project(g, 0, 0.0, e.s);
-    e.cull_set(g, 1, S);
+    abd::launch_project(g, 0, 0.0, s);  // reference positions x(q_t)
+    e.cull_set(g, 1, S);                // positions x(q_{t+1}) and their pair set
+    // J's exact part, kept aside, and the frame Jacobians of the friction forces
     abd::Params Pe = e.P;
     Pe.psd = 0;
     Pe.damp = 0;
     Pe.exact = 1;
     Pe.terms = abd::TERM_ALL;
-    abd::assemble(g, Pe, S, e.nbufs, e.s);
-    e.put_on(std::vector<char>(e.ns, 1));
-    // J^T w = gq_next with J = H + C by the fixed point H w_{k+1} = gq_next - C^T w_k
-    std::vector<double> w(n, 0.0), y(n), gf(n), mass(nb), Ic(nb), ctw(n, 0.0), rhs(n), wprev(n);
-    int st = 0;
-    for (int it = 0; it < 50; ++it) {
-      for (size_t k = 0; k < n; ++k) rhs[k] = gq_next[k] - ctw[k];
-      CK(cudaMemcpyAsync(e.nbufs.grad.p, rhs.data(), n * sizeof(double), cudaMemcpyHostToDevice, e.s));
-      abd::pcg_solve(g, S, e.nbufs, e.solve_opts(), e.sc_on.p, std::vector<char>(e.ns, 1), e.dq.p, e.s, &st,
-                     nullptr);
-      if (st == ABD_ERR_NOT_SPD) return st;
-      wprev = w;
-      CK(cudaMemcpyAsync(w.data(), e.nbufs.x.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
-      CK(cudaStreamSynchronize(e.s));
-      if (!(e.P.mu > 0.0 && e.cfg.ground && e.cfg.vg_fric && S.nvg > 0)) break;
-      double dn = 0.0, wn = 0.0;
-      for (size_t k = 0; k < n; ++k) {
-        dn += (w[k] - wprev[k]) * (w[k] - wprev[k]);
-        wn += w[k] * w[k];
-      }
-      if (it > 0 && dn <= 1e-24 * wn) break;  // w settled to ~1e-12 relative
-      abd::vg_lag_adjoint(g, Pe, S, e.nbufs.x.p, e.nbufs.qv.p, e.s);  // PCG scratch between solves
-      CK(cudaMemcpyAsync(ctw.data(), e.nbufs.qv.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
-      CK(cudaStreamSynchronize(e.s));
+    abd::assemble(g, Pe, S, B, s);
+    const int nov = S.nov;
+    B.D_ex.ensure(144 * (size_t)nb);
+    B.ovr_ex.ensure((size_t)abd::CONTRIB * nov + 1);
+    B.has_ex.ensure(nov + 1);
+    CK(cudaMemcpyAsync(B.D_ex.p, B.D.p, 144 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (nov) {
+      CK(cudaMemcpyAsync(B.ovr_ex.p, B.ovr.p, (size_t)abd::CONTRIB * nov * sizeof(double), cudaMemcpyDeviceToDevice,
+                         s));
+      CK(cudaMemcpyAsync(B.has_ex.p, B.has.p, nov * sizeof(int), cudaMemcpyDeviceToDevice, s));
     }
-    // friction terms alone at mu = 1: K w and r_friction / mu
+    abd::fric_frame_jacobians(g, Pe, S, B, s);
+    const bool vg_coupling = e.P.mu > 0.0 && e.cfg.ground && e.cfg.vg_fric && S.nvg > 0;
+    // the preconditioner: the forward step's (projected, undamped) Newton matrix
+    abd::Params Pp = e.P;
+    Pp.psd = 1;
+    Pp.damp = 0;
+    Pp.exact = 0;
+    Pp.terms = abd::TERM_ALL;
+    abd::assemble(g, Pp, S, B, s);
+    e.put_on(std::vector<char>(e.ns, 1));
+    abd::SolveOpts po = e.solve_opts();
+    po.rel_tol = 1e-10;
+    po.refine = 0;
+    po.dense = 0;
+    const std::vector<char> all_on(e.ns, 1);
+    const int m = 40, max_restarts = 12;
+    B.adj_V.ensure((size_t)(m + 1) * n);
+    B.adj_Z.ensure((size_t)m * n);
+    B.adj_w.ensure(n);
+    B.adj_t.ensure(n);
+    B.adj_x.ensure(n);
+    double* V = B.adj_V.p;
+    double* Z = B.adj_Z.p;
+    double* wv = B.adj_w.p;
+    double* tv = B.adj_t.p;
+    double* xv = B.adj_x.p;
+    int st = ABD_OK;
+    // out = J^T z
+    auto apply = [&](const double* z, double* out) {
+      abd::spmv_blocks(g, S, B.has_ex.p, B.ovr_ex.p, B.D_ex.p, z, out, s);
+      if (vg_coupling) {
+        abd::vg_lag_adjoint(g, Pe, S, z, tv, s);
+        abd::dev_axpby(n, 1.0, tv, 1.0, out, s);
+      }
+      abd::fric_frame_apply_t(g, S, B, z, tv, s);
+      abd::dev_axpby(n, 1.0, tv, 1.0, out, s);
+    };
+    // z = P^-1 v by the PCG on the preconditioner's system
+    auto precond = [&](const double* v, double* z) {
+      CK(cudaMemcpyAsync(B.grad.p, v, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      int ps = 0;
+      abd::pcg_solve(g, S, B, po, e.sc_on.p, all_on, e.dq.p, s, &ps, nullptr);
+      if (ps == ABD_ERR_NOT_SPD) st = ABD_ERR_NOT_SPD;
+      CK(cudaMemcpyAsync(z, B.x.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    };
+    CK(cudaMemcpyAsync(V, gq_next, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(xv, 0, n * sizeof(double), s));
+    const double bnorm = std::sqrt(abd::dev_dot(n, V, V, B, s));
+    const double tol = 1e-12 * bnorm;
+    double beta = bnorm;
+    bool converged = bnorm == 0.0;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), gg(m + 1), y(m);
+    for (int rs = 0; rs < max_restarts && !converged && st == ABD_OK; ++rs) {
+      if (rs > 0) {  // restart from the true residual b - J^T x
+        apply(xv, wv);
+        CK(cudaMemcpyAsync(V, gq_next, n * sizeof(double), cudaMemcpyHostToDevice, s));
+        abd::dev_axpby(n, -1.0, wv, 1.0, V, s);
+        beta = std::sqrt(abd::dev_dot(n, V, V, B, s));
+        if (beta <= tol) {
+          converged = true;
+          break;
+        }
+      }
+      abd::dev_axpby(n, 0.0, V, 1.0 / beta, V, s);
+      std::fill(gg.begin(), gg.end(), 0.0);
+      gg[0] = beta;
+      int k = 0;
+      for (; k < m; ++k) {
+        double* vk = V + (size_t)k * n;
+        double* zk = Z + (size_t)k * n;
+        double* vn = V + (size_t)(k + 1) * n;
+        precond(vk, zk);
+        apply(zk, vn);
+        for (int i = 0; i <= k; ++i) {  // modified Gram-Schmidt
+          const double hik = abd::dev_dot(n, vn, V + (size_t)i * n, B, s);
+          H[(size_t)i * m + k] = hik;
+          abd::dev_axpby(n, -hik, V + (size_t)i * n, 1.0, vn, s);
+        }
+        const double hn = std::sqrt(abd::dev_dot(n, vn, vn, B, s));
+        H[(size_t)(k + 1) * m + k] = hn;
+        if (hn > 0.0) abd::dev_axpby(n, 0.0, vn, 1.0 / hn, vn, s);
+        for (int i = 0; i < k; ++i) {  // the earlier rotations on the new column
+          const double a0 = H[(size_t)i * m + k], a1 = H[(size_t)(i + 1) * m + k];
+          H[(size_t)i * m + k] = cs[i] * a0 + sn[i] * a1;
+          H[(size_t)(i + 1) * m + k] = -sn[i] * a0 + cs[i] * a1;
+        }
+        const double a0 = H[(size_t)k * m + k], a1 = H[(size_t)(k + 1) * m + k];
+        const double rr = std::hypot(a0, a1);
+        cs[k] = rr > 0.0 ? a0 / rr : 1.0;
+        sn[k] = rr > 0.0 ? a1 / rr : 0.0;
+        H[(size_t)k * m + k] = rr;
+        H[(size_t)(k + 1) * m + k] = 0.0;
+        gg[k + 1] = -sn[k] * gg[k];
+        gg[k] = cs[k] * gg[k];
+        if (std::fabs(gg[k + 1]) <= tol || hn == 0.0) {
+          ++k;
+          converged = true;
+          break;
+        }
+      }
+      // x += Z y with H y = g (upper triangular, k x k)
+      for (int i = k - 1; i >= 0; --i) {
+        double v = gg[i];
+        for (int j = i + 1; j < k; ++j) v -= H[(size_t)i * m + j] * y[j];
+        y[i] = v / H[(size_t)i * m + i];
+      }
+      for (int i = 0; i < k; ++i) abd::dev_axpby(n, y[i], Z + (size_t)i * n, 1.0, xv, s);
+    }
+    if (st != ABD_OK) return st;
+    if (!converged) st = ABD_ERR_PCG_NOCONV;
+    std::vector<double> w(n), yk(n), gf(n), mass(nb), Ic(nb);
+    CK(cudaMemcpyAsync(w.data(), xv, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    // friction terms alone at mu = 1, frames held: K w and r_friction / mu
     abd::Params Pf = Pe;
     Pf.terms = abd::TERM_FRICTION;
     Pf.mu = 1.0;
-    abd::assemble(g, Pf, S, e.nbufs, e.s);
-    abd::spmv(g, S, e.nbufs, e.nbufs.x.p, e.nbufs.r.p, e.s);
-    CK(cudaMemcpyAsync(y.data(), e.nbufs.r.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
-    CK(cudaMemcpyAsync(gf.data(), e.nbufs.grad.p, n * sizeof(double), cudaMemcpyDeviceToHost, e.s));
-    CK(cudaMemcpyAsync(mass.data(), e.mass.p, nb * sizeof(double), cudaMemcpyDeviceToHost, e.s));
-    CK(cudaMemcpyAsync(Ic.data(), e.Ic.p, nb * sizeof(double), cudaMemcpyDeviceToHost, e.s));
-    CK(cudaStreamSynchronize(e.s));
+    abd::assemble(g, Pf, S, B, s);
+    abd::spmv(g, S, B, xv, B.r.p, s);
+    CK(cudaMemcpyAsync(yk.data(), B.r.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(gf.data(), B.grad.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(mass.data(), e.mass.p, nb * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(Ic.data(), e.Ic.p, nb * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
     double gm = 0.0, mu = e.P.mu, dt = e.P.dt;
     for (int b = 0; b < nb; ++b)
       for (int i = 0; i < 12; ++i) {
@@ -1053,9 +1164,9 @@ int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const
           gv_t[k] = 0.0;
           continue;
         }
-        double m = i < 3 ? mass[b] : Ic[b];
-        gq_t[k] = m * w[k] + mu * y[k];
-        gv_t[k] = dt * m * w[k];
+        double mi = i < 3 ? mass[b] : Ic[b];
+        gq_t[k] = mi * w[k] + mu * yk[k];
+        gv_t[k] = dt * mi * w[k];
         gm -= gf[k] * w[k];
       }
     if (gmu) *gmu = gm;

@@ -2235,6 +2235,12 @@ void spmv(const Geo& g, const PairSet& S, NewtonBufs& B, const double* x, double
                                                                             B.has.p, B.ovr.p, B.D.p, x, y));
 }
 
+void spmv_blocks(const Geo& g, const PairSet& S, const int* has, const double* ovr, const double* D, const double* x,
+                 double* y, cudaStream_t st) {
+  KLAUNCH(K_PCG, st, k_spmv<<<nblk((long long)g.nb * 16, 256), 256, 0, st>>>(g.nb, S.row_ptr.p, S.col.p, S.upidx.p,
+                                                                            has, ovr, D, x, y));
+}
+
 void vg_lag_adjoint(const Geo& g, const Params& P, const PairSet& S, const double* w, double* out, cudaStream_t st) {
   KLAUNCH(K_BODY_SYSTEM, st, k_vg_lag_adj<<<nblk(g.nb, 128), 128, 0, st>>>(g, P, S.vg.p, S.vg_seg.p, w, out));
 }

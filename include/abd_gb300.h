@@ -156,11 +156,12 @@ int abd_set_friction(abd_handle* h, double mu);
 int abd_get_friction(abd_handle* h, double* mu);
 /* Adjoint of one converged frame (no reference counterpart: the reference has no
  * derivatives). The frame maps the frame-start state (q_t, v_t) and mu to q_{t+1}; given
- * gq_next = dL/dq_{t+1} it assembles the exact Jacobian of the frame's optimality condition
- * at q_{t+1} (no PSD projection, no damping, ground-friction multipliers following the
- * vertex heights; point-triangle and edge-edge friction multipliers and tangent bases held
- * fixed), solves it with the block-sparse PCG and returns gq_t = dL/dq_t, gv_t = dL/dv_t
- * and *gmu = dL/dmu (gmu may be NULL). All arrays are n_bodies * 12 host doubles. */
+ * gq_next = dL/dq_{t+1} it solves J^T w = gq_next with J the exact Jacobian of the frame's
+ * optimality condition at q_{t+1} (no PSD projection, no damping; every friction
+ * multiplier and tangent frame following the configuration, as the reference recomputes
+ * them at each Newton iterate) by GMRES preconditioned with the forward Newton matrix,
+ * and returns gq_t = dL/dq_t, gv_t = dL/dv_t and *gmu = dL/dmu (gmu may be NULL). All
+ * arrays are n_bodies * 12 host doubles. */
 int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const double* q_next,
                       const double* gq_next, double* gq_t, double* gv_t, double* gmu);
 /* Batched mode (no reference counterpart: the reference steps one scene per ABD object).

@@ -3,10 +3,9 @@ differences of the oracle's rollout (the CPU restatement of the reference step).
 
 Loss: sum of squared distances of the bodies' translations after the rollout to seeded
 targets. Newton runs to a tight tolerance so that the finite differences resolve the
-converged map. The adjoint is exact without friction and with ground friction (its
-multiplier's dependence on the vertex height is included); the multipliers and tangent
-bases of point-triangle and edge-edge friction are held fixed, so contact friction between
-bodies is not covered by this check."""
+converged map. The adjoint differentiates every friction term through its multiplier and
+tangent frame (ground, point-triangle and edge-edge), so the check covers friction
+between bodies as well as against the ground."""
 import dataclasses
 
 import numpy as np
@@ -43,7 +42,7 @@ def oracle_loss(O, sc, cfg, q0, v0, mu, target, n):
     return float(((q[:, :3] - target) ** 2).sum())
 
 
-@pytest.mark.parametrize("mu,contact_friction,bound", [(0.0, True, 1e-5), (0.3, False, 1e-5)])
+@pytest.mark.parametrize("mu,contact_friction,bound", [(0.0, True, 1e-5), (0.3, False, 1e-5), (0.3, True, 1e-5)])
 def test_adjoint_matches_oracle_finite_differences(O, mu, contact_friction, bound):
     from adb_gb300.abd import ABD
     from adb_gb300.adjoint import rollout
