@@ -35,6 +35,7 @@ def make_abd_config(cfg: Config) -> L.AbdConfig:
     if cfg.solver not in ("sparse", "dense"):
         raise ValueError('solver must be "sparse" or "dense"')
     c.solver = 1 if cfg.solver == "dense" else 0
+    c.max_iter_frame = int(cfg.max_iter_frame)
     return c
 
 
@@ -169,6 +170,12 @@ class ABD:
         if rc not in (0, 6):
             L.check(rc, self._h, "abd_adjoint_frame")
         return gq, gv, gm.value
+
+    def adjoint_stats(self):
+        """(GMRES iterations, final relative residual) of the last adjoint_frame."""
+        it, res = C.c_int(), C.c_double()
+        L.check(L.lib().abd_adjoint_stats(self._h, C.byref(it), C.byref(res)), self._h, "abd_adjoint_stats")
+        return it.value, res.value
 
     # --- per-kernel device timing -----------------------------------------------------
     @property

@@ -109,6 +109,8 @@ struct Engine {
   // view/model_view.cpp:282-295): frame counter, last frame, folder, and the config and
   // scene files copied into a new trace folder
   int ts = 0, starting_ts = -1, ending_ts = 0;
+  int adj_iters = 0;            // GMRES iterations of the last abd_adjoint_frame
+  double adj_residual = 0.0;    // its final relative residual (restart estimate)
   std::string trace_folder = "trace", trace_config, trace_scene;
 
   Geo geo() const {
@@ -402,7 +404,7 @@ struct Engine {
     std::vector<char> act(ns, 1), ls(ns, 0), stalled(ns, 0);
     std::vector<double> dd(3 * ns), sup_dq(ns), tp(ns, 1.0), tg(ns, 1.0), toi(ns, 1.0), fac(ns, 1.0);
     std::vector<double> E0(ns), E1(ns), qdg(ns), gn(ns), dqn(ns), a_cull(ns, 1.0), a_fin(ns, 1.0);
-    std::vector<int> trials(ns, 0), its_s(ns, 0), fin_pass(ns, 0);
+    std::vector<int> trials(ns, 0), its_s(ns, 0), fin_pass(ns, 0), its_f(ns, 0);
     int n_act = ns;
     int status = ABD_OK;
     while (n_act > 0) {
@@ -562,7 +564,9 @@ struct Engine {
       for (int k = 0; k < ns; ++k) {
         if (!act[k]) continue;
         sc_newton[k]++;
+        its_f[k]++;
         bool term = sup_dq[k] < cfg.tol || ++iter[k] >= cfg.max_iter;
+        if (cfg.max_iter_frame > 0 && its_f[k] >= cfg.max_iter_frame) term = true;
         if (term) {
           act[k] = 0;
           --n_act;
@@ -976,6 +980,13 @@ int abd_trace_files(abd_handle* h, const char** config_json, const char** scene_
   return ABD_OK;
 }
 
+int abd_adjoint_stats(abd_handle* h, int* iterations, double* rel_residual) {
+  if (!h) return ABD_ERR_INVALID;
+  if (iterations) *iterations = h->e.adj_iters;
+  if (rel_residual) *rel_residual = h->e.adj_residual;
+  return ABD_OK;
+}
+
 int abd_get_friction(abd_handle* h, double* mu) {
   if (!h || !mu) return ABD_ERR_INVALID;
   *mu = h->e.P.mu;
@@ -1084,6 +1095,8 @@ int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const
     double beta = bnorm;
     bool converged = bnorm == 0.0;
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), gg(m + 1), y(m);
+    int total_its = 0;
+    double last_res = bnorm;
     for (int rs = 0; rs < max_restarts && !converged && st == ABD_OK; ++rs) {
       if (rs > 0) {  // restart from the true residual b - J^T x
         apply(xv, wv);
@@ -1126,6 +1139,8 @@ int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const
         H[(size_t)(k + 1) * m + k] = 0.0;
         gg[k + 1] = -sn[k] * gg[k];
         gg[k] = cs[k] * gg[k];
+        ++total_its;
+        last_res = std::fabs(gg[k + 1]);
         if (std::fabs(gg[k + 1]) <= tol || hn == 0.0) {
           ++k;
           converged = true;
@@ -1140,6 +1155,8 @@ int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const
       }
       for (int i = 0; i < k; ++i) abd::dev_axpby(n, y[i], Z + (size_t)i * n, 1.0, xv, s);
     }
+    e.adj_iters = total_its;
+    e.adj_residual = bnorm > 0.0 ? last_res / bnorm : 0.0;
     if (st != ABD_OK) return st;
     if (!converged) st = ABD_ERR_PCG_NOCONV;
     std::vector<double> w(n), yk(n), gf(n), mass(nb), Ic(nb);

@@ -47,6 +47,7 @@ class Config:
     gravity: bool = True
     ls_grad_tol: float = 1e-3      # line_search.cpp:84 (hard-coded)
     max_iter: int = 1000
+    max_iter_frame: int = 0        # Newton iterations per frame at most (0: unbounded, as the reference)
     ground: bool = True
     pt: bool = True
     ee: bool = True
@@ -133,6 +134,7 @@ def load_config(path: str) -> Config:
     c.pcg_rel_tol = float(d.get("pcg_rel_tol", c.pcg_rel_tol))
     c.pcg_max_iter = int(d.get("pcg_max_iter", c.pcg_max_iter))
     c.pcg_refine = int(d.get("pcg_refine", c.pcg_refine))
+    c.max_iter_frame = int(d.get("max_iter_frame", c.max_iter_frame))
     c.pcg_refine_tol = float(d.get("pcg_refine_tol", c.pcg_refine_tol))
     return c
 
@@ -154,7 +156,7 @@ def config_to_json(c: Config) -> dict:
         "params_int": {"clip": c.clip, "thres": 100},
         "dhat": c.dhat, "ortho_kappa": c.ortho_kappa, "ground_y": -c.ground_offset,
         "pcg_rel_tol": c.pcg_rel_tol, "pcg_max_iter": c.pcg_max_iter,
-        "pcg_refine": c.pcg_refine, "pcg_refine_tol": c.pcg_refine_tol,
+        "pcg_refine": c.pcg_refine, "pcg_refine_tol": c.pcg_refine_tol, "max_iter_frame": c.max_iter_frame,
     }
 
 
@@ -538,13 +540,25 @@ def diff_grid(seed: int = 0, n: int = 4, spacing: float = 1.2, lift: float = 0.6
     return sb.build()
 
 
+def diff_targets(n_bodies: int = 64, seed: int = 0) -> np.ndarray:
+    """Seeded targets of the differentiable-rollout loss: uniform in
+    [-2, 2] x [0.5, 1.5] x [-2, 2] above the ground (shifted to the reference's ground)."""
+    rng = np.random.default_rng(seed)
+    t = rng.uniform((-2.0, 0.5, -2.0), (2.0, 1.5, 2.0), (n_bodies, 3))
+    t[:, 1] += GROUND_SHIFT
+    return t
+
+
 def workload_config(name: str) -> Config:
     """Physical parameters of the named synthetic workloads."""
     c = Config()
     if name in ("cubes", "pile", "batched", "diff"):
         c.dt, c.dhat, c.kappa, c.mu, c.tol = 1e-2, 1e-3, 1e-4, 0.1, 1e-4
         if name == "diff":
+            # mu 0.3: the lagged friction's Newton iteration cycles on some impact frames
+            # (it never reaches tol), so those frames stop after 100 iterations
             c.mu = 0.3
+            c.max_iter_frame = 100
     elif name == "chain":
         c.dt, c.dhat, c.kappa, c.mu, c.tol, c.ground = 5e-3, 1e-4, 1e-4, 0.2, 1e-4, False
     c.max_iter = 1 << 30

@@ -81,6 +81,10 @@ typedef struct {
    * system), 1 "dense" (the scene's full 12 n x 12 n matrix factorized by a dense Cholesky,
    * as the reference's big_hess.ldlt(), abd.cpp:233-264; for small scenes) */
   int solver;
+  /* Newton iterations per frame at most, per scene (0: unbounded, as the reference's loop,
+   * which only has the cumulative max_iter). No reference counterpart: it bounds frames
+   * whose lagged-friction Newton iteration cycles instead of converging. */
+  int max_iter_frame;
 } abd_config;
 
 /* Scene: bodies with their rest meshes (local vertex ids per body). */
@@ -164,6 +168,8 @@ int abd_get_friction(abd_handle* h, double* mu);
  * arrays are n_bodies * 12 host doubles. */
 int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const double* q_next,
                       const double* gq_next, double* gq_t, double* gv_t, double* gmu);
+/* GMRES iterations and final relative residual of the handle's last abd_adjoint_frame. */
+int abd_adjoint_stats(abd_handle* h, int* iterations, double* rel_residual);
 /* Batched mode (no reference counterpart: the reference steps one scene per ABD object).
  * Number of scenes of the handle, and per-scene counts (arrays of that length, any may be
  * NULL) accumulated over the frames of the last abd_step call, plus each scene's

@@ -40,6 +40,9 @@ struct Config {
   // "damping": {enable, alpha, beta} (view/control.cpp:35, 60-61)
   int damp;
   double damp_alpha, damp_beta;
+  // Newton iterations per frame at most (0: unbounded, the reference's loop); a library
+  // option for frames whose lagged-friction iteration cycles
+  int max_iter_frame;
 };
 
 struct I4 {
@@ -1403,6 +1406,7 @@ static int implicit_euler(Scene& s) {
     st.t_ls += t4 - t3;
     st.newton_iters++;
     term = sup_dq < s.cfg.tol || ++s.iter >= s.cfg.max_iter;
+    if (s.cfg.max_iter_frame > 0 && st.newton_iters >= s.cfg.max_iter_frame) term = true;
   } while (!term);
   ++s.iter;  // abd.cpp:121 increments the counter once more per frame
   for (auto& c : s.b) {

@@ -27,7 +27,7 @@ class OracleConfig(C.Structure):
             "max_iter", "ground", "pt", "ee", "psd", "line_search", "upper_bound", "vg_fric", "pt_fric",
             "ee_fric", "clip", "n_threads")] + [(n, C.c_double) for n in ("safe_factor", "sh_min_xyz", "sh_dx")] + [
         (n, C.c_int) for n in ("iaabb", "full_ccd", "sh_bits", "sh_fix_edge", "damp")] + [
-        (n, C.c_double) for n in ("damp_alpha", "damp_beta")]
+        (n, C.c_double) for n in ("damp_alpha", "damp_beta")] + [("max_iter_frame", C.c_int)]
 
 
 class OracleStats(C.Structure):
@@ -109,6 +109,7 @@ def make_config(cfg, n_threads: int = 0) -> OracleConfig:
     c.backoff, c.c1, c.tol, c.max_uk, c.dq_tol = cfg.backoff, cfg.c1, cfg.tol, cfg.max_uk, cfg.dq_tol
     c.gravity_y, c.ls_grad_tol = cfg.gravity_y, cfg.ls_grad_tol
     c.max_iter = min(int(cfg.max_iter), 2 ** 31 - 1)
+    c.max_iter_frame = int(getattr(cfg, "max_iter_frame", 0))
     c.ground, c.pt, c.ee, c.psd = int(cfg.ground), int(cfg.pt), int(cfg.ee), int(cfg.psd)
     c.line_search, c.upper_bound = int(cfg.line_search), int(cfg.upper_bound)
     c.vg_fric, c.pt_fric, c.ee_fric = int(cfg.vg_friction), int(cfg.pt_friction), int(cfg.ee_friction)

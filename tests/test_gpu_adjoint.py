@@ -25,7 +25,7 @@ def O(gpu_lib, oracle_lib):
 def setup(mu, contact_friction=True):
     sc = S.diff_grid(seed=1, n=2, spacing=1.05, lift=0.56)
     cfg = dataclasses.replace(S.workload_config("diff"), mu=mu, tol=1e-12, pt_friction=contact_friction,
-                              ee_friction=contact_friction)
+                              ee_friction=contact_friction, max_iter_frame=0)
     rng = np.random.default_rng(7)
     target = sc.q0[:, :3] + rng.uniform(-0.3, 0.3, (sc.n_bodies, 3))
     v0 = np.zeros_like(sc.q0)
@@ -119,3 +119,73 @@ def test_interleaved_rollouts_keep_their_own_friction(gpu_lib):
     both = grads([0.0, 0.3], together=True)
     for (ga, ma), (gb, mb) in zip(alone, both):
         assert np.array_equal(ga, gb) and ma == mb
+
+
+def test_adjoint_state_and_affine_velocity_directions(O):
+    """Directions in every component of the initial velocities (translation and affine
+    blocks) and of the initial state q0 (translations and affine entries), with contact
+    friction between bodies (mu 0.3), against central differences of the oracle."""
+    from adb_gb300.abd import ABD
+    from adb_gb300.adjoint import rollout
+    mu = 0.3
+    sc, cfg, target, v0 = setup(mu, True)
+    n = 12
+    sim = ABD(sc, cfg)
+    q0t = torch.tensor(sc.q0, dtype=torch.float64, requires_grad=True)
+    v0t = torch.tensor(v0, dtype=torch.float64, requires_grad=True)
+    qT, _ = rollout(sim, q0t, v0t, torch.tensor(mu, dtype=torch.float64), n, every=4)
+    loss = ((qT[:, :3] - torch.tensor(target)) ** 2).sum()
+    loss.backward()
+    rng = np.random.default_rng(9)
+    h = 1e-5
+    pairs = []
+    for which in ("v0", "v0", "q0", "q0"):
+        d = rng.normal(size=v0.shape)
+        if which == "q0":
+            d[:, 3:] *= 0.1   # affine entries: a small shear / scale next to the translations
+        d /= np.linalg.norm(d)
+        if which == "v0":
+            fd = (oracle_loss(O, sc, cfg, sc.q0, v0 + h * d, mu, target, n) -
+                  oracle_loss(O, sc, cfg, sc.q0, v0 - h * d, mu, target, n)) / (2 * h)
+            ad = float((v0t.grad.numpy() * d).sum())
+        else:
+            fd = (oracle_loss(O, sc, cfg, sc.q0 + h * d, v0, mu, target, n) -
+                  oracle_loss(O, sc, cfg, sc.q0 - h * d, v0, mu, target, n)) / (2 * h)
+            ad = float((q0t.grad.numpy() * d).sum())
+        print("adjoint %s direction: %.10g fd %.10g" % (which, ad, fd))
+        pairs.append((which, ad, fd))
+    for which in ("v0", "q0"):
+        sel = [(ad, fd) for w, ad, fd in pairs if w == which]
+        scale = max(abs(fd) for _, fd in sel)
+        for ad, fd in sel:
+            assert abs(ad - fd) <= 1e-5 * scale, (which, ad, fd, scale)
+
+
+def test_full_size_rollout_checkpointing():
+    """The differentiable-rollout workload at full size: 64 subdivision-2 icospheres,
+    mu 0.3, 100 steps; gradients of the seeded-target loss with respect to the 64 x 12
+    initial affine velocities and mu. Checkpointing every 10 frames (the backward pass
+    recomputes the frames between checkpoints) must give the gradients of keeping every
+    frame bit for bit, and the simulation must come back with its state and friction."""
+    from adb_gb300.abd import ABD
+    from adb_gb300.adjoint import rollout
+    sc = S.diff_grid(seed=0)
+    cfg = S.workload_config("diff")
+    tgt = torch.tensor(S.diff_targets(sc.n_bodies, seed=0))
+    out = []
+    for every in (1, 10):
+        sim = ABD(sc, cfg)
+        v0t = torch.zeros(sc.q0.shape, dtype=torch.float64, requires_grad=True)
+        mut = torch.tensor(cfg.mu, dtype=torch.float64, requires_grad=True)
+        qT, _ = rollout(sim, torch.tensor(sc.q0), v0t, mut, 100, every=every)
+        loss = ((qT[:, :3] - tgt) ** 2).sum()
+        before = sim.state()
+        loss.backward()
+        after = sim.state()
+        assert np.array_equal(before[0], after[0]) and sim.friction == cfg.mu
+        assert np.isfinite(v0t.grad.numpy()).all() and np.isfinite(float(mut.grad))
+        out.append((float(loss.detach()), v0t.grad.numpy().copy(), float(mut.grad)))
+        sim.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1]) and out[0][2] == out[1][2]
+    assert np.abs(out[0][1]).max() > 0.0
