@@ -200,6 +200,111 @@ def adjoint_cost(n_steps=100, every=10):
             "backward_over_forward": t_bwd / t_fwd, "dL_dmu": float(mu.grad)}
 
 
+def kernel_roofline(sim, frames, fp64_peak):
+    """Profiled pass of `frames` frames from the simulation's current state: per-kernel
+    device time (CUDA events around every launch on the engine's stream), and for the
+    dominant kernel its algorithmic bytes per launch over its average launch time against
+    the measured HBM copy bandwidth, its DRAM traffic per launch (ncu bytes per unit from
+    the committed profile summary times the units per launch) and its FP64 rate."""
+    sim.profile(True)
+    sim.step(frames)
+    kt = sim.kernel_times()
+    sim.profile(False)
+    tot = sum(v["ms"] for v in kt.values())
+    dom = max(kt, key=lambda k: kt[k]["ms"])
+    d = kt[dom]
+    peak, peak_kind = measured_peaks()
+    avg_ms = d["ms"] / max(d["launches"], 1)
+    bytes_per_launch = d["bytes"] / max(d["launches"], 1)
+    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    tpu = ncu_per_unit(dom)
+    traffic = tpu * d["units"] / max(d["launches"], 1) if tpu else None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": traffic, "avg_launch_ms": avg_ms, "launches": d["launches"],
+            "share": d["ms"] / tot if tot else None}
+    # the dominant kernels of this FP64 path are bound by FP64 issue, not by HBM: their
+    # FP64 rate (flops per unit from one ncu capture x units per launch / live launch
+    # time) against the measured FP64 FMA peak
+    fpu = ncu_per_unit(dom, "fp64_flops_per_unit")
+    fp64_roof = None
+    if fpu and avg_ms > 0:
+        gf = fpu * d["units"] / max(d["launches"], 1) / (avg_ms * 1e-3) / 1e9
+        fp64_roof = {"achieved_gflops": gf, "peak_gflops": fp64_peak, "frac": gf / fp64_peak,
+                     "flops_per_unit": fpu, "source": "executed DFMA x2 + DADD + DMUL per unit (ncu), live time"}
+    return roof, fp64_roof, kt
+
+
+def chain_line(frames=300, fp64_peak=None):
+    """The 200-link chain (48 x 24 tori, dt 0.005, dhat 1e-4, mu 0.2, ground off, link 0
+    static) over its first `frames` frames from rest: timed with the state resident (CUDA
+    events), again through the C ABI with host buffers every frame (e2e), then a profiled
+    pass of 5 frames from the state at 80% of the run for the dominant kernel. The CPU
+    restatement is timed on one frame at each of three states of the GPU trajectory (20%,
+    50% and 80% of the run; the early frames carry no contact and are cheaper) on all host
+    cores, and its rate is the inverse of their mean frame time."""
+    import ctypes as C
+    from adb_gb300 import _lib as L
+    from adb_gb300 import scene as S
+    from adb_gb300.abd import ABD
+    from oracle import oracle as O
+    sc, cfg = S.torus_chain(seed=0), S.workload_config("chain")
+    sim = ABD(sc, cfg)
+    q0, qd = sim.state()
+    marks = {int(frames * 0.2), int(frames * 0.5), int(frames * 0.8)}
+    states = {}
+    dev_ms, newton, trials, mpt, mee = 0.0, 0, 0, 0, 0
+    for f in range(frames):
+        if f in marks:
+            states[f] = sim.state() + (sim.iter,)
+        st = sim.step(1)
+        dev_ms += st.device_ms
+        newton += st.newton_iters
+        trials += st.ls_trials
+        mpt, mee = max(mpt, st.n_pt), max(mee, st.n_ee)
+    value = frames / (dev_ms / 1000.0)
+    sim.set_state(q0, qd)
+    sim.iter = 0
+    lib = L.lib()
+    hq, hqd = np.ascontiguousarray(q0), np.ascontiguousarray(qd)
+    outq, outqd = np.zeros_like(hq), np.zeros_like(hqd)
+    est = L.AbdFrameStats()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        lib.abd_set_state(sim._h, L.dptr(hq), L.dptr(hqd))
+        lib.abd_step(sim._h, 0.0, 1, C.byref(est))
+        lib.abd_get_state(sim._h, L.dptr(outq), L.dptr(outqd))
+        hq, hqd = outq.copy(), outqd.copy()
+    e2e = frames / (time.perf_counter() - t0)
+    late = max(marks)
+    sim.set_state(states[late][0], states[late][1])
+    sim.iter = states[late][2]
+    roof, fp64_roof, kt = kernel_roofline(sim, 5, fp64_peak or 0.0)
+    sim.close()
+    cores = os.cpu_count() or 1
+    secs = []
+    for f in sorted(marks):
+        orc = O.OracleSim(sc, cfg, n_threads=cores)
+        orc.set_state(states[f][0], states[f][1])
+        orc.iter = states[f][2]
+        t0 = time.perf_counter()
+        orc.step(1)
+        secs.append(time.perf_counter() - t0)
+    return {"workload": "chain-200 torus 48x24, frames 1-%d from rest" % frames, "bodies": sc.n_bodies,
+            "vertices": sc.n_vertices, "dt": cfg.dt, "dhat": cfg.dhat, "mu": cfg.mu, "value": value,
+            "unit": "frames/s", "steps": frames, "ms_per_step": dev_ms / frames,
+            "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": hq.nbytes + hqd.nbytes,
+                    "d2h_bytes_per_step": outq.nbytes + outqd.nbytes},
+            "roofline": roof, "fp64": fp64_roof,
+            "frame_stats": {"newton_iters": newton, "ls_trials": trials, "max_pt": mpt, "max_ee": mee},
+            "kernel_ms_profiled_5_frames": {k: round(v["ms"], 3) for k, v in
+                                            sorted(kt.items(), key=lambda kv: -kv[1]["ms"]) if v["ms"] > 0},
+            "cpu_baseline": {"value": len(secs) / sum(secs), "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": "frames %s of the GPU trajectory, one each, all host cores (%s s)" % (
+                                 ", ".join(str(f + 1) for f in sorted(marks)),
+                                 ", ".join("%.2f" % x for x in secs))}}
+
+
 def cpu_baseline_sample(sc, cfg, q0, qd, newton_per_frame, ls_per_frame, sample_iters=6):
     """The CPU restatement on all host cores, timed on a bounded sample of one frame.
 
@@ -290,10 +395,15 @@ def run_gb300(args):
         return float(t.item())
 
     # ---- value: W untimed frames, then K frames with the state resident on the device ----
+    # warm-up frames from the checkpoint, then back to it: the timed frames are the
+    # checkpoint's next frames, the same window the reference arm times
     sim.set_state(q0, qd)
+    it0 = sim.iter
     if args.warmup:
         sim.step(args.warmup)
-    start_q, start_qd = sim.state()
+    sim.set_state(q0, qd)
+    sim.iter = it0
+    start_q, start_qd = q0, qd
     barrier()
     with ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if world > 1 else 0) as clk:
         st = sim.step(args.steps)
@@ -304,6 +414,7 @@ def run_gb300(args):
 
     # ---- e2e: same frames through the public API with host buffers ----
     lib = L.lib()
+    sim.iter = it0
     hq = np.ascontiguousarray(start_q)
     hqd = np.ascontiguousarray(start_qd)
     outq = np.zeros_like(hq)
@@ -324,29 +435,9 @@ def run_gb300(args):
 
     # ---- per-kernel device time (separate profiled pass over the same frames) ----
     sim.set_state(start_q, start_qd)
-    sim.profile(True)
-    pst = sim.step(min(args.steps, 5))
-    kt = sim.kernel_times()
-    sim.profile(False)
-    tot = sum(v["ms"] for v in kt.values())
-    dom = max(kt, key=lambda k: kt[k]["ms"])
-    d = kt[dom]
-    peak, peak_kind = measured_peaks()
-    avg_ms = d["ms"] / max(d["launches"], 1)
-    bytes_per_launch = d["bytes"] / max(d["launches"], 1)
-    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
-    tpu = ncu_per_unit(dom)
-    traffic = tpu * d["units"] / max(d["launches"], 1) if tpu else None
+    sim.iter = it0
     fp64_peak = measure_fp64_gflops()
-    # the dominant kernels of this FP64 path are bound by FP64 issue, not by HBM: their
-    # FP64 rate (flops per unit from one ncu capture x units per launch / live launch
-    # time) against the measured FP64 FMA peak
-    fpu = ncu_per_unit(dom, "fp64_flops_per_unit")
-    fp64_roof = None
-    if fpu and avg_ms > 0:
-        gf = fpu * d["units"] / max(d["launches"], 1) / (avg_ms * 1e-3) / 1e9
-        fp64_roof = {"achieved_gflops": gf, "peak_gflops": fp64_peak, "frac": gf / fp64_peak,
-                     "flops_per_unit": fpu, "source": "executed DFMA x2 + DADD + DMUL per unit (ncu), live time"}
+    roof, fp64_roof, kt = kernel_roofline(sim, min(args.steps, 5), fp64_peak)
 
     if rank == 0:
         line = {
@@ -361,10 +452,7 @@ def run_gb300(args):
             "clocks": clocks,
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(st.kernel_launches),
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                         "traffic": traffic, "avg_launch_ms": avg_ms, "launches": d["launches"],
-                         "share": d["ms"] / tot if tot else None},
+            "roofline": roof,
             "fp64": {"peak_gflops_measured": fp64_peak, "dominant_kernel": fp64_roof},
             "frame_stats": {"newton_iters": st.newton_iters, "ls_trials": st.ls_trials, "pcg_iters": st.pcg_iters,
                             "max_pt": st.n_pt, "max_ee": st.n_ee, "max_vg": st.n_vg,
@@ -373,6 +461,7 @@ def run_gb300(args):
                           if v["ms"] > 0},
         }
         if not args.no_batched:
+            line["chain"] = chain_line(fp64_peak=fp64_peak)
             line["batched"] = batched_vs_looped()
             try:
                 line["adjoint"] = adjoint_cost()
