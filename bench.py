@@ -207,7 +207,7 @@ def kernel_roofline(sim, frames, fp64_peak):
     the measured HBM copy bandwidth, its DRAM traffic per launch (ncu bytes per unit from
     the committed profile summary times the units per launch) and its FP64 rate."""
     sim.profile(True)
-    sim.step(frames)
+    pst = sim.step(frames)
     kt = sim.kernel_times()
     sim.profile(False)
     tot = sum(v["ms"] for v in kt.values())
@@ -222,7 +222,10 @@ def kernel_roofline(sim, frames, fp64_peak):
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": traffic, "avg_launch_ms": avg_ms, "launches": d["launches"],
-            "share": d["ms"] / tot if tot else None}
+            "share": d["ms"] / tot if tot else None,
+            # kernel time against the device time of the same profiled frames: the rest
+            # is the GPU waiting on the host (synchronisations and launches)
+            "profiled_frames": frames, "profiled_kernel_ms": tot, "profiled_device_ms": pst.device_ms}
     # the dominant kernels of this FP64 path are bound by FP64 issue, not by HBM: their
     # FP64 rate (flops per unit from one ncu capture x units per launch / live launch
     # time) against the measured FP64 FMA peak
