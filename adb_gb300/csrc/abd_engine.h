@@ -182,6 +182,12 @@ void launch_project(const Geo& g, int which, double alpha, cudaStream_t s);
 void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs, PairSet& out, double* toi_p,
           double* toi_g, cudaStream_t s);
 
+// Line-search cull at q + alpha dq (per-scene steps of g) that reuses the overlaps and the
+// refined primitive lists of the trajectory cull H of the same step (vtn 3 over q -> q + dq
+// with the step not yet scaled down): the pair set equals that of a full vtn 2 cull.
+void cull_trial(const Geo& g, const Params& P, double alpha, CullScratch& cs, const PairSet& H, PairSet& out,
+                cudaStream_t s);
+
 // Vertex-ground pairs (d = (y + ground_offset)^2 < P.dhat) into S.vg / S.vg_seg.
 void vg_pairs(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, cudaStream_t s);
 void vg_count(const Geo& g, const Params& P, CullScratch& cs, cudaStream_t s);

@@ -1158,6 +1158,62 @@ void launch_project(const Geo& g, int which, double alpha, cudaStream_t s) {
   prof_work(K_PROJECT, g.nv, 48.0 * g.nv);  // rest read + world write per vertex
 }
 
+// Narrow phase of a pair cull over binned (and refined, ordered) lists of nov overlaps:
+// classification with staging (grown and repeated when it overflows), per-overlap counts
+// and offsets, one host read of the totals (pt, ee, vg, staged, unstaged overlaps), then
+// the ordered write of the pairs into S.
+static void narrow_pairs(const Geo& g, const Params& P, float ds_f, int nov, const int* ovI, const int* ovJ,
+                         CullScratch& cs, PairSet& S, int& npt, int& nee, cudaStream_t s) {
+  int* d_tot = cs.tmp_int.p;
+  cs.blk_a.ensure(nov + 1);
+  cs.blk_b.ensure(nov + 1);
+  cs.blk_a_off.ensure(nov + 1);
+  cs.blk_b_off.ensure(nov + 1);
+  cs.sub_cnt.ensure(3 * (size_t)nov + 3);
+  cs.stage_off.ensure(nov + 1);
+  if (cs.stage_key.cap < (1u << 16)) {
+    cs.stage_key.ensure(1u << 16);
+    cs.stage_ty.ensure(1u << 16);
+  }
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    CK(cudaMemsetAsync(d_tot + 6, 0, 2 * sizeof(int), s));
+    narrow_smem_attr();
+    KLAUNCH(K_NARROW_SCAN, s, k_narrow_scan<0><<<nov, NT, narrow_smem(0), s>>>(g, P, ds_f, ovI, ovJ, cs.bin_cnt.p,
+                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
+                                                                    cs.fbox.p, cs.sub_cnt.p, nullptr, cs.stage_key.p,
+                                                                    cs.stage_ty.p, cs.stage_off.p, d_tot + 6,
+                                                                    (int)cs.stage_key.cap, cs.order.p));
+    // per-overlap pair counts and their offsets, read together with the staged total
+    KLAUNCH(K_NARROW_WRITE, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
+    scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
+    scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
+    CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 5 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if ((size_t)cs.h_small[6] <= cs.stage_key.cap) break;
+    // staging overflowed: grow to the reported total and classify again
+    cs.stage_key.ensure((size_t)cs.h_small[6] + (cs.h_small[6] >> 2) + 1024);
+    cs.stage_ty.ensure(cs.stage_key.cap);
+  }
+  npt = cs.h_small[3];
+  nee = cs.h_small[4];
+  prof_work(K_NARROW_SCAN, nov, 24.0 * g.nv + 20.0 * ((double)npt + nee));
+  S.pt.ensure(4 * (size_t)npt + 4);
+  S.pt_ty.ensure(npt + 1);
+  S.pt_ov.ensure(npt + 1);
+  S.ee.ensure(4 * (size_t)nee + 4);
+  S.ee_ty.ensure(nee + 1);
+  S.ee_ov.ensure(nee + 1);
+  NarrowOut no{S.pt.p, S.pt_ov.p, S.ee.p, S.ee_ov.p, S.pt_ty.p, S.ee_ty.p};
+  KLAUNCH(K_NARROW_WRITE, s, k_narrow_copy<<<nov, 128, 0, s>>>(nov, ovI, ovJ, cs.bin_off.p, cs.lst.p, cs.sub_cnt.p,
+                                                                cs.stage_key.p, cs.stage_ty.p, cs.stage_off.p,
+                                                                cs.blk_a_off.p, cs.blk_b_off.p, no));
+  if (cs.h_small[7] > 0)  // some overlap was not staged: the recomputing pass writes it
+    KLAUNCH(K_NARROW_WRITE, s, k_narrow_write<<<nov, NT, 0, s>>>(g, P, ds_f, ovI, ovJ, cs.bin_cnt.p, cs.bin_off.p,
+                                                                  cs.lst.p, cs.vbox.p, cs.ebox.p, cs.fbox.p,
+                                                                  cs.sub_cnt.p, cs.blk_a_off.p, cs.blk_b_off.p, no,
+                                                                  cs.stage_off.p));
+}
+
 void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& cs, PairSet& out, double* toi_p,
           double* toi_g, cudaStream_t s) {
   Geo g = g_in;
@@ -1251,7 +1307,6 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
                                                         cs.ebox.p, cs.fbox.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p));
   }
   float ds_f = float_round_up(P.d_sqrt);
-  NarrowOut no{};
   if (traj) {
     const int nk = 2 * g.ns;
     cs.toi_key.ensure(nk);
@@ -1266,7 +1321,11 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
     KLAUNCH(K_VG_TOI, s, k_fill_u64<<<nblk(nk, 256), 256, 0, s>>>(cs.toi_key.p, nk, b | 0x8000000000000000ull));
     if (nov > 0) {
       prof_work(K_NARROW_TOI, nov, 48.0 * g.nv);  // positions at q and q + dq
-      KLAUNCH(K_NARROW_TOI, s, k_refine<false><<<nblk(3ll * nov * 32, 256), 256, 0, s>>>(g, ds_f, nov, S.ovI.p,
+      // refined with the A boxes inflated by sqrt(dhat): a little looser than the TOI
+      // needs (its box phase is not inflated, so the TOIs are unchanged), and the lists
+      // then hold every candidate of every configuration on the trajectory, which the
+      // line-search culls of this step reuse (cull_trial)
+      KLAUNCH(K_NARROW_TOI, s, k_refine<true><<<nblk(3ll * nov * 32, 256), 256, 0, s>>>(g, ds_f, nov, S.ovI.p,
                                                                                          S.ovJ.p, cs.bin_cnt.p,
                                                                                          cs.bin_off.p, cs.lst.p,
                                                                                          cs.vbox.p, cs.ebox.p,
@@ -1292,62 +1351,64 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
   // 5. narrow phase per overlap: counts, scan, ordered write
   int npt = 0, nee = 0;
   if (nov > 0) {
-    cs.blk_a.ensure(nov + 1);
-    cs.blk_b.ensure(nov + 1);
-    cs.blk_a_off.ensure(nov + 1);
-    cs.blk_b_off.ensure(nov + 1);
-    cs.sub_cnt.ensure(3 * (size_t)nov + 3);
-    cs.stage_off.ensure(nov + 1);
-    if (cs.stage_key.cap < (1u << 16)) {
-      cs.stage_key.ensure(1u << 16);
-      cs.stage_ty.ensure(1u << 16);
-    }
     KLAUNCH(K_NARROW_SCAN, s, k_refine<true><<<nblk(3ll * nov * 32, 256), 256, 0, s>>>(g, ds_f, nov, S.ovI.p,
                                                                                        S.ovJ.p, cs.bin_cnt.p,
                                                                                        cs.bin_off.p, cs.lst.p,
                                                                                        cs.vbox.p, cs.ebox.p, cs.fbox.p));
     order_overlaps(nov, cs, s, K_NARROW_SCAN);
-    for (int attempt = 0; attempt < 4; ++attempt) {
-      CK(cudaMemsetAsync(d_tot + 6, 0, 2 * sizeof(int), s));
-      narrow_smem_attr();
-      KLAUNCH(K_NARROW_SCAN, s, k_narrow_scan<0><<<nov, NT, narrow_smem(0), s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
-                                                                      cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
-                                                                      cs.fbox.p, cs.sub_cnt.p, nullptr, cs.stage_key.p,
-                                                                      cs.stage_ty.p, cs.stage_off.p, d_tot + 6,
-                                                                      (int)cs.stage_key.cap, cs.order.p));
-      // per-overlap pair counts and their offsets, read together with the staged total
-      KLAUNCH(K_NARROW_WRITE, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
-      scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
-      scan_exclusive_int(cs.blk_b.p, cs.blk_b_off.p, nov, d_tot + 4, s, cs.vflag_cnt);
-      CK(cudaMemcpyAsync(cs.h_small + 3, d_tot + 3, 5 * sizeof(int), cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      if ((size_t)cs.h_small[6] <= cs.stage_key.cap) break;
-      // staging overflowed: grow to the reported total and classify again
-      cs.stage_key.ensure((size_t)cs.h_small[6] + (cs.h_small[6] >> 2) + 1024);
-      cs.stage_ty.ensure(cs.stage_key.cap);
-    }
-    npt = cs.h_small[3];
-    nee = cs.h_small[4];
-    prof_work(K_NARROW_SCAN, nov, 24.0 * g.nv + 20.0 * ((double)npt + nee));
-    S.pt.ensure(4 * (size_t)npt + 4);
-    S.pt_ty.ensure(npt + 1);
-    S.pt_ov.ensure(npt + 1);
-    S.ee.ensure(4 * (size_t)nee + 4);
-    S.ee_ty.ensure(nee + 1);
-    S.ee_ov.ensure(nee + 1);
-    no = NarrowOut{S.pt.p, S.pt_ov.p, S.ee.p, S.ee_ov.p, S.pt_ty.p, S.ee_ty.p};
-    KLAUNCH(K_NARROW_WRITE, s, k_narrow_copy<<<nov, 128, 0, s>>>(nov, S.ovI.p, S.ovJ.p, cs.bin_off.p, cs.lst.p,
-                                                                  cs.sub_cnt.p, cs.stage_key.p, cs.stage_ty.p,
-                                                                  cs.stage_off.p, cs.blk_a_off.p, cs.blk_b_off.p, no));
-    if (cs.h_small[7] > 0)  // some overlap was not staged: the recomputing pass writes it
-      KLAUNCH(K_NARROW_WRITE, s, k_narrow_write<<<nov, NT, 0, s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
-                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
-                                                                    cs.fbox.p, cs.sub_cnt.p, cs.blk_a_off.p,
-                                                                    cs.blk_b_off.p, no, cs.stage_off.p));
+    narrow_pairs(g, P, ds_f, nov, S.ovI.p, S.ovJ.p, cs, S, npt, nee, s);
   }
   S.npt = npt;
   S.nee = nee;
   // 6. vertex-ground pairs (counted before the overlaps were read)
+  vg_write(g, P, cs, S, nvg, s);
+}
+
+// Line-search cull at q + alpha dq over the broad phase of this step's trajectory cull H
+// (its overlaps, and its lists binned with trajectory boxes and refined with the A boxes
+// inflated by sqrt(dhat)): every configuration on the trajectory has its body overlaps
+// among H's and its candidates among H's lists, and the lists keep primitive order, so
+// the narrow phase at the trial configuration yields the pair set, in the order, that a
+// full cull would (overlaps without pairs are extra, empty ones).
+void cull_trial(const Geo& g_in, const Params& P, double alpha, CullScratch& cs, const PairSet& H, PairSet& out,
+                cudaStream_t s) {
+  Geo g = g_in;
+  const int nb = g.nb, nov = H.nov, nnz = H.nnz;
+  launch_project(g, 2, alpha, s);
+  vg_count(g, P, cs, s);
+  PairSet& S = out;
+  S.row_ptr.ensure(nb + 1);
+  S.col.ensure(nnz + 1);
+  S.upidx.ensure(nnz + 1);
+  S.ovI.ensure(nov + 1);
+  S.ovJ.ensure(nov + 1);
+  CK(cudaMemcpyAsync(S.row_ptr.p, H.row_ptr.p, (nb + 1) * sizeof(int), cudaMemcpyDeviceToDevice, s));
+  if (nnz) {
+    CK(cudaMemcpyAsync(S.col.p, H.col.p, nnz * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(S.upidx.p, H.upidx.p, nnz * sizeof(int), cudaMemcpyDeviceToDevice, s));
+  }
+  if (nov) {
+    CK(cudaMemcpyAsync(S.ovI.p, H.ovI.p, nov * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(S.ovJ.p, H.ovJ.p, nov * sizeof(int), cudaMemcpyDeviceToDevice, s));
+  }
+  S.nnz = nnz;
+  S.nov = nov;
+  if (g.nv > 0) KLAUNCH(K_PRIM_BOXES, s, k_vert_boxes<<<nblk(g.nv, 256), 256, 0, s>>>(g, 0, cs.vbox.p));
+  if (g.ne + g.nf > 0) {
+    KLAUNCH(K_PRIM_BOXES, s, k_prim_boxes<<<nblk((long long)g.ne + g.nf, 256), 256, 0, s>>>(g, cs.vbox.p, cs.ebox.p,
+                                                                                             cs.fbox.p));
+  }
+  int npt = 0, nee = 0, nvg = 0;
+  if (nov > 0) {
+    narrow_pairs(g, P, float_round_up(P.d_sqrt), nov, S.ovI.p, S.ovJ.p, cs, S, npt, nee, s);
+    nvg = cs.h_small[5];
+  } else {
+    CK(cudaMemcpyAsync(cs.h_small + 5, cs.tmp_int.p + 5, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    nvg = cs.h_small[5];
+  }
+  S.npt = npt;
+  S.nee = nee;
   vg_write(g, P, cs, S, nvg, s);
 }
 

@@ -437,12 +437,14 @@ struct Engine {
       auto t2 = clk::now();
       // CCD step bound (abd.cpp:142-196)
       for (int k = 0; k < ns; ++k) toi[k] = 1.0;
+      bool hull = false;  // the iAABB trajectory cull of this step can serve the trial culls
       if (cfg.upper_bound && cfg.iaabb <= 1) {
         // step_size_upper_bound (upper_bound.cpp:16-277)
         sh_bound(ga, P, sh, S, shw, cs, toi.data(), s);
         st.bytes_moved += 96.0 * nv;
       } else if (cfg.upper_bound) {
         cull(ga, P, 3, 1.0, cs, sets[2], tp.data(), tg.data(), s);
+        hull = cfg.iaabb % 2 == 1;
         st.bytes_moved += 96.0 * nv + 20.0 * sets[2].nov;
         for (int k = 0; k < ns; ++k) {
           if (!act[k]) continue;
@@ -502,7 +504,9 @@ struct Engine {
         while (n_ls > 0) {
           put_mask(sc_search, h_search, ls);
           put_alpha(a_cull);
-          cull_set(gt, 2, sets[other]);
+          // trial positions lie on the trajectory the CCD culled: its broad phase is reused
+          if (hull) cull_trial(gt, P, 1.0, cs, sets[2], sets[other], s);
+          else cull_set(gt, 2, sets[other]);
           energy(gt, P, 0.0, sets[other], S, true, nbufs, s, E1.data());
           ++pass;
           st.bytes_moved += bytes_cull(sets[other]) + 48.0 * nv + 116.0 * (sets[other].npt + sets[other].nee);
