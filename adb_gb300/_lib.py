@@ -30,7 +30,8 @@ class AbdConfig(C.Structure):
                     "sh_xyz_bits", "sh_fix_edge_trajectory")] + [("dq_tol", C.c_double), ("damping", C.c_int),
                                                                  ("damp_alpha", C.c_double), ("damp_beta", C.c_double),
                                                                  ("pcg_refine", C.c_int), ("pcg_refine_tol", C.c_double),
-                                                                 ("solver", C.c_int), ("max_iter_frame", C.c_int)]
+                                                                 ("solver", C.c_int), ("max_iter_frame", C.c_int),
+                                                                 ("autotune", C.c_int)]
 
 
 class AbdSceneDesc(C.Structure):
@@ -81,6 +82,7 @@ def lib():
         L.abd_get_friction.argtypes = [H, C.POINTER(C.c_double)]
         L.abd_adjoint_frame.argtypes = [H, _D, _D, _D, _D, _D, _D, C.POINTER(C.c_double)]
         L.abd_adjoint_stats.argtypes = [H, _I, _D]
+        L.abd_autotune_info.argtypes = [H, _I, _D]
         L.abd_get_scene_count.argtypes = [H]
         L.abd_get_scene_stats.argtypes = [H, _I, _I, _I, _I]
         L.abd_last_error.restype = C.c_char_p
@@ -112,7 +114,7 @@ def lib():
 
 # Every symbol include/abd_gb300.h declares (checked by the CPU test suite).
 EXPORTED = ["abd_create", "abd_create_from_files", "abd_step", "abd_get_state", "abd_set_state", "abd_trace_save", "abd_trace_load", "abd_set_trace", "abd_get_trace", "abd_trace_files", "abd_run", "abd_get_counts",
-            "abd_get_iter", "abd_set_iter", "abd_get_scene_count", "abd_get_scene_stats", "abd_set_friction", "abd_get_friction", "abd_adjoint_frame", "abd_adjoint_stats", "abd_last_error", "abd_destroy", "abd_profile", "abd_kernel_times", "abd_kernel_work", "abd_cull", "abd_get_pairs",
+            "abd_get_iter", "abd_set_iter", "abd_get_scene_count", "abd_get_scene_stats", "abd_set_friction", "abd_get_friction", "abd_adjoint_frame", "abd_adjoint_stats", "abd_autotune_info", "abd_last_error", "abd_destroy", "abd_profile", "abd_kernel_times", "abd_kernel_work", "abd_cull", "abd_get_pairs",
             "abd_newton_system", "abd_newton_dq", "abd_energy", "abd_ipc_hess_pt_batch", "abd_ipc_hess_ee_batch",
             "abd_pt_collision_time_batch", "abd_ee_collision_time_batch", "abd_pt_distance_batch",
             "abd_ee_distance_batch", "abd_pt_min_toi_noalloc", "abd_noalloc_last_error", "abd_measure_fp64_gflops"]

@@ -36,6 +36,7 @@ def make_abd_config(cfg: Config) -> L.AbdConfig:
         raise ValueError('solver must be "sparse" or "dense"')
     c.solver = 1 if cfg.solver == "dense" else 0
     c.max_iter_frame = int(cfg.max_iter_frame)
+    c.autotune = int(cfg.autotune)
     return c
 
 
@@ -170,6 +171,15 @@ class ABD:
         if rc not in (0, 6):
             L.check(rc, self._h, "abd_adjoint_frame")
         return gq, gv, gm.value
+
+    def autotune_info(self) -> dict:
+        """Narrow-phase variants the autotuner chose (box-phase steps; 0 = not tuned yet)
+        and the times it measured, for the pair cull and the CCD."""
+        steps = np.zeros(2, np.int32)
+        ms = np.zeros(6)
+        L.check(L.lib().abd_autotune_info(self._h, L.iptr(steps), L.dptr(ms)), self._h, "abd_autotune_info")
+        return {"pair_cull": {"step": int(steps[0]), "variant_ms": [round(float(x), 4) for x in ms[:3]]},
+                "ccd": {"step": int(steps[1]), "variant_ms": [round(float(x), 4) for x in ms[3:]]}}
 
     def adjoint_stats(self):
         """(GMRES iterations, final relative residual) of the last adjoint_frame."""

@@ -118,6 +118,11 @@ struct CullScratch {
   DBuf<unsigned long long> toi_key;     // 2 per scene: pt/ee, ground
   DBuf<int> tmp_int;
   DBuf<long long> tmp_ll;
+  // autotuned narrow-phase variants (index into the step table; -1 = not tuned yet) of the
+  // pair cull [0] and the CCD [1], and the times measured when tuning
+  int autotune = 1;
+  int narrow_variant[2] = {-1, -1};
+  float narrow_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};
   int* h_small = nullptr;               // pinned host scratch
   long long* h_ll = nullptr;
   unsigned long long* h_toi = nullptr;
@@ -187,6 +192,9 @@ void cull(const Geo& g, const Params& P, int vtn, double alpha, CullScratch& cs,
 // with the step not yet scaled down): the pair set equals that of a full vtn 2 cull.
 void cull_trial(const Geo& g, const Params& P, double alpha, CullScratch& cs, const PairSet& H, PairSet& out,
                 cudaStream_t s);
+
+// Box-phase length of narrow-phase variant `variant` of mode 0 (pair cull) or 2 (CCD).
+int narrow_step_of(int mode, int variant);
 
 // Vertex-ground pairs (d = (y + ground_offset)^2 < P.dhat) into S.vg / S.vg_seg.
 void vg_pairs(const Geo& g, const Params& P, CullScratch& cs, PairSet& S, cudaStream_t s);

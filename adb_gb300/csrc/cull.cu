@@ -337,16 +337,20 @@ __global__ void __launch_bounds__(256, 3) k_bin(Geo g, int nov, int pass, int tr
 constexpr int NT = 256;     // narrow-phase threads per CTA
 constexpr int TILE = 384;   // primitives of one list staged in shared memory (2 x 9 kB)
 constexpr int REC_CAP = 2048;  // accepted pairs of one overlap kept in shared memory for sorting
-// Box-phase candidates per thread between two exact phases, and the queue of float-box
-// hits they fill: 64 (a 64 kB queue, two CTAs per SM) for the pair cull; 36 for the CCD,
-// whose smaller queue lets three CTAs share an SM (its time-of-impact tests gain more
-// from the extra CTAs than from the longer box phases).
-__host__ __device__ constexpr int narrow_step(int mode) { return mode == 2 ? 36 : 64; }
-__host__ __device__ constexpr int narrow_qcap(int mode) { return NT * narrow_step(mode); }
-// dynamic shared memory of k_narrow_scan<MODE>: boxes, queue, accepted pairs (MODE 0)
+// Box-phase candidates per thread between two exact phases (STEP), and the queue of
+// float-box hits they fill (NT * STEP entries). A longer box phase runs the exact phase
+// less often; a shorter one leaves shared memory for more CTAs per SM. The result does not
+// depend on STEP (accepted pairs are sorted by key before they are written, TOIs are
+// min-reduced), so the autotuner picks among these variants by time: pair cull (mode 0)
+// 32 / 64 / 96, CCD (mode 2) 24 / 36 / 64; the defaults are the middle ones (measured
+// fastest on the pile when the choice was fixed).
+constexpr int kNarrowVariants = 3;
+constexpr int kNarrowStep[2][kNarrowVariants] = {{32, 64, 96}, {24, 36, 64}};
+constexpr int kNarrowDefault = 1;
+// dynamic shared memory of k_narrow_scan<MODE, STEP>: boxes, queue, accepted pairs (MODE 0)
 // (MODE 0 also stages the vertex ids of the staged primitives: 2 per A entry, 3 per B)
-__host__ __device__ constexpr size_t narrow_smem(int mode) {
-  return 2 * TILE * 6 * sizeof(float) + narrow_qcap(mode) * sizeof(unsigned) +
+__host__ __device__ constexpr size_t narrow_smem(int mode, int step) {
+  return 2 * TILE * 6 * sizeof(float) + (size_t)NT * step * sizeof(unsigned) +
          (mode == 0 ? REC_CAP * (sizeof(unsigned long long) + 1) + 5 * TILE * sizeof(int) : 0);
 }
 
@@ -750,8 +754,8 @@ __global__ void k_order_place(int nov, const int* cnt, int* bc, int* order) {
 //    float-box hits to a shared queue (warp-aggregated);
 //  - exact phase: the whole CTA takes the queued candidates round-robin for the exact
 //    FP64 test (MODE 0: box, lower bounds, type and distance; MODE 2: time of impact).
-template <int MODE>
-__global__ void __launch_bounds__(NT, MODE == 2 ? 3 : 2) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
+template <int MODE, int STEP>
+__global__ void __launch_bounds__(NT, (MODE == 2 && STEP <= 36) ? 3 : 2) k_narrow_scan(Geo g, Params P, float ds_f, const int* ovI, const int* ovJ,
                                                     int* cnt, const int* off, int* lst, const float* vb,
                                                     const float* eb, const float* fb, int* sub_cnt,
                                                     unsigned long long* toi_key, unsigned long long* stage_key,
@@ -762,8 +766,7 @@ __global__ void __launch_bounds__(NT, MODE == 2 ? 3 : 2) k_narrow_scan(Geo g, Pa
   float* sA = reinterpret_cast<float*>(smem_dyn + (MODE == 0 ? REC_CAP * sizeof(unsigned long long) : 0));
   float* sB = sA + TILE * 6;
   unsigned int* sq = reinterpret_cast<unsigned int*>(sB + TILE * 6);
-  constexpr int STEP = narrow_step(MODE);
-  int8_t* recT = reinterpret_cast<int8_t*>(sq + narrow_qcap(MODE));
+  int8_t* recT = reinterpret_cast<int8_t*>(sq + NT * STEP);
   int* sVA = MODE == 0 ? reinterpret_cast<int*>(recT + REC_CAP) : nullptr;  // 2 * TILE (MODE 0)
   int* sVB = MODE == 0 ? sVA + 2 * TILE : nullptr;                           // 3 * TILE (MODE 0)                         // REC_CAP (MODE 0)
   __shared__ int sq_n[2];
@@ -1122,10 +1125,90 @@ static void narrow_smem_attr() {
   int dev = 0;
   CK(cudaGetDevice(&dev));
   if (done_dev == dev) return;
-  CK(cudaFuncSetAttribute(k_narrow_scan<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(0)));
-  CK(cudaFuncSetAttribute(k_narrow_scan<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(2)));
+#define ABD_NARROW_ATTR(M, ST) \
+  CK(cudaFuncSetAttribute(k_narrow_scan<M, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(M, ST)))
+  ABD_NARROW_ATTR(0, 32);
+  ABD_NARROW_ATTR(0, 64);
+  ABD_NARROW_ATTR(0, 96);
+  ABD_NARROW_ATTR(2, 24);
+  ABD_NARROW_ATTR(2, 36);
+  ABD_NARROW_ATTR(2, 64);
+#undef ABD_NARROW_ATTR
   done_dev = dev;
 }
+
+// Arguments of one narrow-phase launch.
+struct NarrowLaunch {
+  Geo g;
+  Params P;
+  float ds_f;
+  const int *ovI, *ovJ;
+  int* cnt;
+  const int* off;
+  int* lst;
+  const float *vb, *eb, *fb;
+  int* sub_cnt;
+  unsigned long long *toi_key, *stage_key;
+  int8_t* stage_ty;
+  int *stage_off, *stage_total;
+  int stage_cap;
+  const int* order;
+};
+
+// k_narrow_scan<mode, kNarrowStep[mode][variant]> over nov overlaps
+static void launch_narrow(int mode, int variant, int nov, const NarrowLaunch& a, cudaStream_t s) {
+  const int tag = mode == 2 ? K_NARROW_TOI : K_NARROW_SCAN;
+#define ABD_NARROW_LAUNCH(M, ST)                                                                                   \
+  KLAUNCH(tag, s, k_narrow_scan<M, ST><<<nov, NT, narrow_smem(M, ST), s>>>(                                       \
+                      a.g, a.P, a.ds_f, a.ovI, a.ovJ, a.cnt, a.off, a.lst, a.vb, a.eb, a.fb, a.sub_cnt, a.toi_key, \
+                      a.stage_key, a.stage_ty, a.stage_off, a.stage_total, a.stage_cap, a.order))
+  const int st = kNarrowStep[mode == 2 ? 1 : 0][variant];
+  if (mode == 2) {
+    if (st == 24) ABD_NARROW_LAUNCH(2, 24);
+    else if (st == 36) ABD_NARROW_LAUNCH(2, 36);
+    else ABD_NARROW_LAUNCH(2, 64);
+  } else {
+    if (st == 32) ABD_NARROW_LAUNCH(0, 32);
+    else if (st == 64) ABD_NARROW_LAUNCH(0, 64);
+    else ABD_NARROW_LAUNCH(0, 96);
+  }
+#undef ABD_NARROW_LAUNCH
+}
+
+// The narrow phase of `mode` (0: pair cull, 1 in the tables: CCD) with the handle's
+// chosen variant. The first launch with at least kTuneMinOverlaps overlaps runs every
+// variant on the same input, timed with CUDA events, keeps the fastest for the life of
+// the handle and leaves the outputs of the last run (all variants give the same outputs;
+// `reset`, when given, clears the pair cull's staging counters before each run).
+constexpr int kTuneMinOverlaps = 64;
+static void narrow_phase(int mode, int nov, const NarrowLaunch& a, CullScratch& cs, int* reset, cudaStream_t s) {
+  const int m = mode == 2 ? 1 : 0;
+  if (cs.narrow_variant[m] >= 0 || !cs.autotune || nov < kTuneMinOverlaps) {
+    launch_narrow(mode, cs.narrow_variant[m] >= 0 ? cs.narrow_variant[m] : kNarrowDefault, nov, a, s);
+    return;
+  }
+  cudaEvent_t ev[kNarrowVariants + 1];
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  CK(cudaEventRecord(ev[0], s));
+  for (int v = 0; v < kNarrowVariants; ++v) {
+    if (reset) CK(cudaMemsetAsync(reset, 0, 2 * sizeof(int), s));
+    launch_narrow(mode, v, nov, a, s);
+    CK(cudaEventRecord(ev[v + 1], s));
+  }
+  CK(cudaEventSynchronize(ev[kNarrowVariants]));
+  int best = kNarrowDefault;
+  for (int v = 0; v < kNarrowVariants; ++v) {
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, ev[v], ev[v + 1]));
+    cs.narrow_ms[m][v] = t;
+    if (t < cs.narrow_ms[m][best]) best = v;
+  }
+  // the default keeps ties and near-ties (within 3%)
+  if (!(cs.narrow_ms[m][best] < 0.97f * cs.narrow_ms[m][kNarrowDefault])) best = kNarrowDefault;
+  cs.narrow_variant[m] = best;
+  for (auto& e : ev) CK(cudaEventDestroy(e));
+}
+
 
 // Fills cs.order with the overlaps heaviest bucket first (k_order_count / k_order_place).
 static void order_overlaps(int nov, CullScratch& cs, cudaStream_t s, int tag) {
@@ -1150,6 +1233,8 @@ double key_to_double(unsigned long long k) {
 }
 
 }  // namespace
+
+int narrow_step_of(int mode, int variant) { return kNarrowStep[mode == 2 ? 1 : 0][variant]; }
 
 void launch_project(const Geo& g, int which, double alpha, cudaStream_t s) {
   if (which == 2 && g.nb > 0) KLAUNCH(K_PROJECT, s, k_trial_state<<<nblk(12ll * g.nb, 256), 256, 0, s>>>(g, alpha));
@@ -1178,11 +1263,10 @@ static void narrow_pairs(const Geo& g, const Params& P, float ds_f, int nov, con
   for (int attempt = 0; attempt < 4; ++attempt) {
     CK(cudaMemsetAsync(d_tot + 6, 0, 2 * sizeof(int), s));
     narrow_smem_attr();
-    KLAUNCH(K_NARROW_SCAN, s, k_narrow_scan<0><<<nov, NT, narrow_smem(0), s>>>(g, P, ds_f, ovI, ovJ, cs.bin_cnt.p,
-                                                                    cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
-                                                                    cs.fbox.p, cs.sub_cnt.p, nullptr, cs.stage_key.p,
-                                                                    cs.stage_ty.p, cs.stage_off.p, d_tot + 6,
-                                                                    (int)cs.stage_key.cap, cs.order.p));
+    NarrowLaunch a{g, P, ds_f, ovI, ovJ, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p, cs.fbox.p,
+                   cs.sub_cnt.p, nullptr, cs.stage_key.p, cs.stage_ty.p, cs.stage_off.p, d_tot + 6,
+                   (int)cs.stage_key.cap, cs.order.p};
+    narrow_phase(0, nov, a, cs, d_tot + 6, s);
     // per-overlap pair counts and their offsets, read together with the staged total
     KLAUNCH(K_NARROW_WRITE, s, k_sub_totals<<<nblk(nov, 256), 256, 0, s>>>(nov, cs.sub_cnt.p, cs.blk_a.p, cs.blk_b.p));
     scan_exclusive_int(cs.blk_a.p, cs.blk_a_off.p, nov, d_tot + 3, s, cs.vflag_cnt);
@@ -1332,10 +1416,9 @@ void cull(const Geo& g_in, const Params& P, int vtn, double alpha, CullScratch& 
                                                                                          cs.fbox.p));
       order_overlaps(nov, cs, s, K_NARROW_TOI);
       narrow_smem_attr();
-      KLAUNCH(K_NARROW_TOI, s, k_narrow_scan<2><<<nov, NT, narrow_smem(2), s>>>(g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p,
-                                                                   cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
-                                                                   cs.fbox.p, nullptr, cs.toi_key.p, nullptr, nullptr,
-                                                                   nullptr, nullptr, 0, cs.order.p));
+      NarrowLaunch a{g, P, ds_f, S.ovI.p, S.ovJ.p, cs.bin_cnt.p, cs.bin_off.p, cs.lst.p, cs.vbox.p, cs.ebox.p,
+                     cs.fbox.p, nullptr, cs.toi_key.p, nullptr, nullptr, nullptr, nullptr, 0, cs.order.p};
+      narrow_phase(2, nov, a, cs, nullptr, s);
     }
     if (P.ground && g.nv) {
       KLAUNCH(K_VG_TOI, s, k_vg_toi<<<nblk(g.nv, 256), 256, 0, s>>>(g, P, cs.toi_key.p + 1));

@@ -228,6 +228,7 @@ struct Engine {
              d->face_off[b + 1] - d->face_off[b] <= 32767;
       if (!ok) throw std::invalid_argument("spatial hashing: at most 32767 bodies and 32767 primitives per body");
     }
+    cs.autotune = c->autotune;
     CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     nb = d->n_bodies;
     nv = d->vert_off[nb];
@@ -981,6 +982,17 @@ int abd_trace_files(abd_handle* h, const char** config_json, const char** scene_
   if (!h) return ABD_ERR_INVALID;
   if (config_json) *config_json = h->e.trace_config.empty() ? nullptr : h->e.trace_config.c_str();
   if (scene_json) *scene_json = h->e.trace_scene.empty() ? nullptr : h->e.trace_scene.c_str();
+  return ABD_OK;
+}
+
+int abd_autotune_info(abd_handle* h, int* steps, double* ms) {
+  if (!h) return ABD_ERR_INVALID;
+  const abd::CullScratch& cs = h->e.cs;
+  for (int m = 0; m < 2; ++m) {
+    if (steps) steps[m] = cs.narrow_variant[m] >= 0 ? abd::narrow_step_of(m ? 2 : 0, cs.narrow_variant[m]) : 0;
+    if (ms)
+      for (int v = 0; v < 3; ++v) ms[3 * m + v] = cs.narrow_ms[m][v];
+  }
   return ABD_OK;
 }
 

@@ -243,9 +243,10 @@ extern "C" int abd_create_from_files(const char* config_json, const char* scene_
   c.max_uk = pd ? pd->num("max_uk", 0.0) : 0.0;
   c.gravity_y = cfgj.flag("gravity", true) ? -9.8 : 0.0;
   c.ls_grad_tol = 1e-3;
-  c.pcg_rel_tol = cfgj.num("pcg_rel_tol", 1e-14);
+  c.pcg_rel_tol = cfgj.num("pcg_rel_tol", 1e-11);
   c.max_iter = (int)cfgj.num("max_iter", 1000);
   c.max_iter_frame = (int)cfgj.num("max_iter_frame", 0);
+  c.autotune = cfgj.flag("autotune", true);
   c.ground = cfgj.flag("ground", true);
   c.pt = cfgj.flag("pt", true);
   c.ee = cfgj.flag("ee", true);

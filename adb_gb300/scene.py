@@ -48,6 +48,7 @@ class Config:
     ls_grad_tol: float = 1e-3      # line_search.cpp:84 (hard-coded)
     max_iter: int = 1000
     max_iter_frame: int = 0        # Newton iterations per frame at most (0: unbounded, as the reference)
+    autotune: bool = True          # narrow-phase launch variants chosen by timing (results unchanged)
     ground: bool = True
     pt: bool = True
     ee: bool = True
@@ -71,7 +72,7 @@ class Config:
     damp_beta: float = 2.5e-2
     solver: str = "sparse"         # "solver": "sparse" (block-Jacobi PCG) or "dense" (per-scene dense Cholesky)
     # GPU solver controls (no reference counterpart: the reference factorizes directly)
-    pcg_rel_tol: float = 1e-14
+    pcg_rel_tol: float = 1e-11
     pcg_max_iter: int = 5000
     pcg_refine: int = 0            # iterative-refinement passes after the PCG (true residual)
     pcg_refine_tol: float = 1e-8   # relative tolerance of each correction solve
@@ -135,6 +136,7 @@ def load_config(path: str) -> Config:
     c.pcg_max_iter = int(d.get("pcg_max_iter", c.pcg_max_iter))
     c.pcg_refine = int(d.get("pcg_refine", c.pcg_refine))
     c.max_iter_frame = int(d.get("max_iter_frame", c.max_iter_frame))
+    c.autotune = bool(d.get("autotune", c.autotune))
     c.pcg_refine_tol = float(d.get("pcg_refine_tol", c.pcg_refine_tol))
     return c
 
@@ -156,7 +158,7 @@ def config_to_json(c: Config) -> dict:
         "params_int": {"clip": c.clip, "thres": 100},
         "dhat": c.dhat, "ortho_kappa": c.ortho_kappa, "ground_y": -c.ground_offset,
         "pcg_rel_tol": c.pcg_rel_tol, "pcg_max_iter": c.pcg_max_iter,
-        "pcg_refine": c.pcg_refine, "pcg_refine_tol": c.pcg_refine_tol, "max_iter_frame": c.max_iter_frame,
+        "pcg_refine": c.pcg_refine, "pcg_refine_tol": c.pcg_refine_tol, "max_iter_frame": c.max_iter_frame, "autotune": c.autotune,
     }
 
 

@@ -462,6 +462,7 @@ def run_gb300(args):
                             "algorithmic_GB": st.bytes_moved / 1e9},
             "kernel_ms": {k: round(v["ms"], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1]["ms"])
                           if v["ms"] > 0},
+            "autotune": sim.autotune_info(),
         }
         if not args.no_batched:
             line["chain"] = chain_line(fp64_peak=fp64_peak)

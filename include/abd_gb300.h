@@ -85,6 +85,10 @@ typedef struct {
    * which only has the cumulative max_iter). No reference counterpart: it bounds frames
    * whose lagged-friction Newton iteration cycles instead of converging. */
   int max_iter_frame;
+  /* 1: the first large cull of each narrow phase (pair cull, CCD) times its launch
+   * variants on the same input and keeps the fastest for the handle (results do not
+   * depend on the variant); 0: the default variants. No reference counterpart. */
+  int autotune;
 } abd_config;
 
 /* Scene: bodies with their rest meshes (local vertex ids per body). */
@@ -168,6 +172,10 @@ int abd_get_friction(abd_handle* h, double* mu);
  * arrays are n_bodies * 12 host doubles. */
 int abd_adjoint_frame(abd_handle* h, const double* q_t, const double* v_t, const double* q_next,
                       const double* gq_next, double* gq_t, double* gv_t, double* gmu);
+/* Autotuner choices of the handle: box-phase steps of the pair-cull and CCD narrow phases
+ * (steps[0], steps[1]; 0 while not tuned) and the times of the three variants measured
+ * when tuning (ms[0..2] pair cull, ms[3..5] CCD; 0 while not tuned). */
+int abd_autotune_info(abd_handle* h, int* steps, double* ms);
 /* GMRES iterations and final relative residual of the handle's last abd_adjoint_frame. */
 int abd_adjoint_stats(abd_handle* h, int* iterations, double* rel_residual);
 /* Batched mode (no reference counterpart: the reference steps one scene per ABD object).
