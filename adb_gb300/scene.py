@@ -344,6 +344,22 @@ class Scene:
                      edges=np.array(self.edges[eo[b0]:eo[b1]]), face_off=(fo[b0:b1 + 1] - fo[b0]).astype(np.int32),
                      faces=np.array(self.faces[fo[b0]:fo[b1]]), scene_id=None)
 
+    def scenes_of_rank(self, rank: int, world: int) -> "Scene":
+        """The scenes of one rank when a batch is sharded by scene over `world` processes:
+        scene k goes to rank k % world (independent scenes need no exchange), in order, with
+        scene ids renumbered from 0."""
+        ranges = [r for k, r in enumerate(self.scene_ranges()) if k % world == rank]
+        parts = [self.body_range(b0, b1) for b0, b1 in ranges]
+        if not parts:
+            raise ValueError("rank %d of %d holds no scene" % (rank, world))
+        out = parts[0]
+        for k, p in enumerate(parts[1:], 1):
+            out = concat_scenes(out, p)
+        if len(parts) > 1 or self.scene_id is not None:
+            sid = np.concatenate([np.full(p.n_bodies, k, np.int32) for k, p in enumerate(parts)])
+            out = dataclasses.replace(out, scene_id=sid)
+        return out
+
     def scene_ranges(self):
         """(first body, end body) of each scene, in order (one range without scene ids)."""
         if self.scene_id is None:
@@ -351,6 +367,18 @@ class Scene:
         sid = np.asarray(self.scene_id)
         cuts = [0] + [int(i) for i in np.nonzero(sid[1:] != sid[:-1])[0] + 1] + [self.n_bodies]
         return list(zip(cuts[:-1], cuts[1:]))
+
+
+def concat_scenes(a: "Scene", b: "Scene") -> "Scene":
+    """Bodies of a then b as one scene (scene ids dropped)."""
+    return Scene(q0=np.concatenate([a.q0, b.q0]), dqdt=np.concatenate([a.dqdt, b.dqdt]),
+                 mass=np.concatenate([a.mass, b.mass]), Ic=np.concatenate([a.Ic, b.Ic]),
+                 vert_off=np.concatenate([a.vert_off, a.vert_off[-1] + b.vert_off[1:]]).astype(np.int32),
+                 rest=np.concatenate([a.rest, b.rest]),
+                 edge_off=np.concatenate([a.edge_off, a.edge_off[-1] + b.edge_off[1:]]).astype(np.int32),
+                 edges=np.concatenate([a.edges, b.edges]),
+                 face_off=np.concatenate([a.face_off, a.face_off[-1] + b.face_off[1:]]).astype(np.int32),
+                 faces=np.concatenate([a.faces, b.faces]), scene_id=None)
 
 
 class SceneBuilder:

@@ -41,6 +41,35 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def dist_barrier(world):
+    """Host barrier of the ranks (abd_step returns after synchronising its stream, so a
+    host barrier orders the ranks' device work too)."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def dist_max(x, world):
+    """Largest x over the ranks (the job's time is its slowest rank's)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def pile_workload():
     from adb_gb300 import scene as S
     sc = S.sphere_pile(seed=0)
@@ -124,25 +153,29 @@ def ncu_per_unit(kernel, key="traffic_per_unit"):
     return None
 
 
-def batched_vs_looped(frames=5, warm_frames=30, n_scenes=256, loop_budget_s=30.0):
+def batched_vs_looped(frames=5, warm_frames=30, n_scenes=256, loop_budget_s=30.0, rank=0, world=1):
     """The batched half of the metric: 256 independent scenes stepped in one handle
     against the same scenes stepped one handle at a time, from the same state, at the same
     Newton tolerance. Both sides are timed on the wall clock around the step calls (every
     step call ends with a stream synchronisation). The looped side steps the scenes in
     order until its time budget is spent (at least 8 scenes); its rate is the scene-frames
     it finished over its time, and its final states are compared bit for bit with the
-    batched run."""
+    batched run. With several ranks the batch is sharded by scene (scene k on rank k %
+    world, no exchange): each rank steps its shard in one handle, the batched rate is all
+    scenes over the slowest rank's time, and each rank loops its own shard's scenes."""
     from adb_gb300 import scene as S
     from adb_gb300.abd import ABD
-    sc = S.batched_scenes(n_scenes=n_scenes, seed=0)
+    full = S.batched_scenes(n_scenes=n_scenes, seed=0)
+    sc = full.scenes_of_rank(rank, world) if world > 1 else full
     cfg = S.workload_config("batched")
     bat = ABD(sc, cfg)
     bat.step(warm_frames)                     # falling bodies reach their first contacts
     q0, qd = bat.state()
     it0 = bat.scene_stats()["iter"].copy()
+    dist_barrier(world)
     t0 = time.perf_counter()
     bst = bat.step(frames)
-    t_bat = time.perf_counter() - t0
+    t_bat = dist_max(time.perf_counter() - t0, world)
     bq, bqd = bat.state()
     bat.close()
     ranges = sc.scene_ranges()
@@ -160,9 +193,11 @@ def batched_vs_looped(frames=5, warm_frames=30, n_scenes=256, loop_budget_s=30.0
         same = same and bool(np.array_equal(q, bq[b0:b1]) and np.array_equal(qdd, bqd[b0:b1]))
         h.close()
         looped += 1
-    bat_rate = len(ranges) * frames / t_bat
-    loop_rate = looped * frames / t_loop
-    return {"scenes": len(ranges), "bodies": sc.n_bodies, "vertices": sc.n_vertices, "frames": frames,
+    bat_rate = len(full.scene_ranges()) * frames / t_bat
+    loop_rate = dist_sum(looped * frames / t_loop, world)   # the ranks loop at the same time
+    same = dist_sum(0.0 if same else 1.0, world) == 0.0
+    return {"scenes": len(full.scene_ranges()), "bodies": full.n_bodies, "vertices": full.n_vertices,
+            "frames": frames, "ranks": world,
             "start": "frame %d of the seeded batch" % warm_frames,
             "batched_scenes_per_s": bat_rate, "looped_scenes_per_s": loop_rate,
             "looped_sample": "first %d of %d scenes (%.1f s)" % (looped, len(ranges), t_loop),
@@ -383,19 +418,10 @@ def run_gb300(args):
     sim = ABD(sc, cfg)
 
     def barrier():
-        # abd_step returns after synchronising its stream, so a host barrier suffices
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        dist_barrier(world)
 
     def max_over_ranks(x):
-        if world == 1:
-            return x
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return dist_max(x, world)
 
     # ---- value: W untimed frames, then K frames with the state resident on the device ----
     # warm-up frames from the checkpoint, then back to it: the timed frames are the
@@ -442,6 +468,9 @@ def run_gb300(args):
     fp64_peak = measure_fp64_gflops()
     roof, fp64_roof, kt = kernel_roofline(sim, min(args.steps, 5), fp64_peak)
 
+    # the batched half runs on every rank (sharded by scene); rank 0 reports it
+    batched = None if args.no_batched else batched_vs_looped(rank=rank, world=world)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
@@ -466,7 +495,7 @@ def run_gb300(args):
         }
         if not args.no_batched:
             line["chain"] = chain_line(fp64_peak=fp64_peak)
-            line["batched"] = batched_vs_looped()
+            line["batched"] = batched
             try:
                 line["adjoint"] = adjoint_cost()
             except ImportError as ex:  # torch missing on this host
