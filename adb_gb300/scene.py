@@ -591,5 +591,8 @@ def workload_config(name: str) -> Config:
             c.max_iter_frame = 100
     elif name == "chain":
         c.dt, c.dhat, c.kappa, c.mu, c.tol, c.ground = 5e-3, 1e-4, 1e-4, 0.2, 1e-4, False
+        # the lagged friction's Newton iteration cycles on a few frames of the 300 (170
+        # and 267 from rest with seed 0): those frames stop after 100 iterations
+        c.max_iter_frame = 100
     c.max_iter = 1 << 30
     return c

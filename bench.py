@@ -291,11 +291,13 @@ def chain_line(frames=300, fp64_peak=None):
     q0, qd = sim.state()
     marks = {int(frames * 0.2), int(frames * 0.5), int(frames * 0.8)}
     states = {}
-    dev_ms, newton, trials, mpt, mee = 0.0, 0, 0, 0, 0
+    dev_ms, newton, trials, mpt, mee, capped = 0.0, 0, 0, 0, 0, []
     for f in range(frames):
         if f in marks:
             states[f] = sim.state() + (sim.iter,)
         st = sim.step(1)
+        if cfg.max_iter_frame and st.newton_iters >= cfg.max_iter_frame:
+            capped.append(f + 1)
         dev_ms += st.device_ms
         newton += st.newton_iters
         trials += st.ls_trials
@@ -334,7 +336,8 @@ def chain_line(frames=300, fp64_peak=None):
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": hq.nbytes + hqd.nbytes,
                     "d2h_bytes_per_step": outq.nbytes + outqd.nbytes},
             "roofline": roof, "fp64": fp64_roof,
-            "frame_stats": {"newton_iters": newton, "ls_trials": trials, "max_pt": mpt, "max_ee": mee},
+            "frame_stats": {"newton_iters": newton, "ls_trials": trials, "max_pt": mpt, "max_ee": mee,
+                            "frames_at_newton_cap": capped, "newton_cap_per_frame": cfg.max_iter_frame},
             "kernel_ms_profiled_5_frames": {k: round(v["ms"], 3) for k, v in
                                             sorted(kt.items(), key=lambda kv: -kv[1]["ms"]) if v["ms"] > 0},
             "cpu_baseline": {"value": len(secs) / sum(secs), "unit": "frames/s", "cores": cores, "kind": "port",
