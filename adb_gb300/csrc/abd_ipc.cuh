@@ -227,23 +227,153 @@ DEV void psd_project(double (&S)[N][N]) {
 // the register allocation of the kernels that contain it.
 static __device__ __noinline__ void psd_project9(double (&S)[9][9]) { psd_project<9>(S); }
 
+// Eigenvector estimate of a small symmetric matrix for psd_project_small: cyclic Jacobi
+// in FP32 on a copy scaled to max |s_ij| = 1, until the off-diagonal mass is ~1e-6 of the
+// total (FP32 rounding level), then the columns re-orthonormalised in FP64 by modified
+// Gram-Schmidt. FP32 arithmetic runs at 64x the FP64 rate on this part, so the sweeps that
+// bring a dense matrix close to diagonal cost little; the FP64 sweeps that follow start
+// from off-diagonals ~1e-7 of the norm and, converging quadratically, stop after about
+// two. Each column's norm^2 = 1 + e with |e| ~ 1e-7 is normalised by the Taylor series
+// (1 + e)^(-1/2) = 1 - e/2 + 3e^2/8 - 5e^3/16 (remainder < 35 e^4 / 128). Returns false
+// (Q untouched) for a zero, non-finite or out-of-FP32-range matrix, or a column whose
+// norm is not within 1e-5 of 1; the caller then starts from the identity.
+template <int N>
+DEV bool jacobi_f32_start(const double (&S)[N][N], double (&Q)[N][N]) {
+  float a[N][N], v[N][N];
+  float mx = 0.f;
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = i; j < N; ++j) {
+      a[i][j] = __double2float_rn(S[i][j]);
+      mx = fmaxf(mx, fabsf(a[i][j]));
+    }
+  if (!(mx > 1e-30f && mx < 1e30f)) return false;
+  const float sc = 1.f / mx;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+#pragma unroll
+    for (int j = i; j < N; ++j) a[i][j] *= sc;
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[i][j] = (i == j) ? 1.f : 0.f;
+  }
+  for (int sweep = 0; sweep < 8; ++sweep) {
+    float off = 0.f, dg = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      dg += a[i][i] * a[i][i];
+#pragma unroll
+      for (int j = i + 1; j < N; ++j) off += a[i][j] * a[i][j];
+    }
+    if (off == 0.f || 2.f * off <= 1e-12f * (dg + 2.f * off)) break;
+#pragma unroll
+    for (int p = 0; p < N - 1; ++p)
+#pragma unroll
+      for (int q = p + 1; q < N; ++q) {
+        float apq = a[p][q];
+        float h = 0.5f * (a[q][q] - a[p][p]);
+        float den = apq != 0.f ? fabsf(h) + sqrtf(h * h + apq * apq) : 0.f;
+        if (den > 0.f) {
+          float t = __fdividef(h >= 0.f ? apq : -apq, den);
+          float c = rsqrtf(1.f + t * t), s = t * c;
+          a[p][p] -= t * apq;
+          a[q][q] += t * apq;
+#pragma unroll
+          for (int k = 0; k < N; ++k) {
+            if (k == p || k == q) continue;
+            float akp = k < p ? a[k][p] : a[p][k];
+            float akq = k < q ? a[k][q] : a[q][k];
+            float np_ = c * akp - s * akq, nq = s * akp + c * akq;
+            if (k < p) a[k][p] = np_;
+            else a[p][k] = np_;
+            if (k < q) a[k][q] = nq;
+            else a[q][k] = nq;
+          }
+#pragma unroll
+          for (int k = 0; k < N; ++k) {
+            float vkp = v[k][p], vkq = v[k][q];
+            v[k][p] = c * vkp - s * vkq;
+            v[k][q] = s * vkp + c * vkq;
+          }
+        }
+        a[p][q] = 0.f;
+      }
+  }
+  double U[N][N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    double u[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) u[i] = (double)v[i][k];
+#pragma unroll
+    for (int j = 0; j < k; ++j) {
+      double d = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) d += U[i][j] * u[i];
+#pragma unroll
+      for (int i = 0; i < N; ++i) u[i] -= d * U[i][j];
+    }
+    double e = -1.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) e += u[i] * u[i];
+    if (!(fabs(e) <= 1e-5)) return false;
+    double r = 1.0 + e * (-0.5 + e * (0.375 - 0.3125 * e));
+#pragma unroll
+    for (int i = 0; i < N; ++i) U[i][k] = u[i] * r;
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < N; ++j) Q[i][j] = U[i][j];
+  return true;
+}
+
 // Eigen-projection of a small symmetric matrix held in registers (fully unrolled
 // cyclic Jacobi on the upper triangle; N <= 5). Returns whether any eigenvalue was
 // negative (then S holds the projection), leaving S untouched otherwise.
-// A rotation annihilating a_pq uses t = sgn(h) a_pq / (|h| + sqrt(h^2 + a_pq^2)) with
-// h = (a_qq - a_pp) / 2, c = 1 / sqrt(1 + t^2), s = t c, and updates the 2x2 block in
-// closed form (a_pp -= t a_pq, a_qq += t a_pq, a_pq = 0): one division and two
-// square-root evaluations per rotation, and only the entries of one triangle.
+// The sweeps run on A = Q^T S Q, Q the orthonormal FP32-Jacobi estimate of the
+// eigenvectors (jacobi_f32_start; the identity when it declines), accumulating the
+// rotations onto Q, until the off-diagonal mass is 1e-32 of the total, as a Jacobi from
+// the identity would. A rotation annihilating a_pq has t = tan(theta) = sgn(h) a_pq /
+// (|h| + r), h = (a_qq - a_pp) / 2, r = sqrt(h^2 + a_pq^2). With g = 1 / r,
+// c^2 = 1 / (1 + t^2) = (|h| + r) / (2 r), so t = sgn(h) a_pq g / (2 c^2) and
+// s = t c = sgn(h) a_pq g / (2 c): two reciprocal square roots per rotation (g and 1 / c),
+// no division. The 2x2 block is updated in closed form (a_pp -= t a_pq, a_qq += t a_pq,
+// a_pq = 0), and only the entries of one triangle. Where h^2 + a_pq^2 is below the
+// normal range the rotation takes t = a_pq / (|h| + r) by division instead. The
+// projection V max(L, 0) V^T is formed on the upper triangle and mirrored.
 template <int N>
 DEV bool psd_project_small(double (&S)[N][N]) {
   double A[N][N], V[N][N];
 #pragma unroll
   for (int i = 0; i < N; ++i)
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      A[i][j] = S[i][j];
-      V[i][j] = (i == j) ? 1.0 : 0.0;
+    for (int j = 0; j < N; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+  if (jacobi_f32_start<N>(S, V)) {
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+      double t[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        double acc = 0;
+#pragma unroll
+        for (int k = 0; k < N; ++k) acc += (i <= k ? S[i][k] : S[k][i]) * V[k][q];
+        t[i] = acc;
+      }
+#pragma unroll
+      for (int p = 0; p <= q; ++p) {
+        double acc = 0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) acc += V[i][p] * t[i];
+        A[p][q] = acc;
+      }
     }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = i; j < N; ++j) A[i][j] = S[i][j];
+  }
   for (int sweep = 0; sweep < 20; ++sweep) {
     double off = 0, dg = 0;
 #pragma unroll
@@ -258,11 +388,25 @@ DEV bool psd_project_small(double (&S)[N][N]) {
 #pragma unroll
       for (int q = p + 1; q < N; ++q) {
         double apq = A[p][q];
-        double h = 0.5 * (A[q][q] - A[p][p]);
-        double den = apq != 0.0 ? fabs(h) + sqrt(h * h + apq * apq) : 0.0;
-        if (den > 0.0) {
-          double t = (h >= 0 ? apq : -apq) / den;
-          double c = rsqrt(1.0 + t * t), s = t * c;
+        if (apq != 0.0) {
+          double h = 0.5 * (A[q][q] - A[p][p]);
+          double sa = h >= 0 ? apq : -apq;
+          double r2 = fma(h, h, apq * apq);
+          double t, c, s;
+          if (r2 >= 1e-300) {
+            double g = rsqrt(r2);
+            double c2 = 0.5 * fma(r2, g, fabs(h)) * g;
+            double ic = rsqrt(c2);
+            double sg = 0.5 * sa * g * ic;
+            c = c2 * ic;
+            s = sg;
+            t = sg * ic;
+          } else {
+            double den = fabs(h) + sqrt(r2);
+            t = den > 0.0 ? sa / den : 0.0;
+            c = rsqrt(1.0 + t * t);
+            s = t * c;
+          }
           A[p][p] -= t * apq;
           A[q][q] += t * apq;
 #pragma unroll
@@ -295,13 +439,16 @@ DEV bool psd_project_small(double (&S)[N][N]) {
   }
   if (!neg) return false;
 #pragma unroll
+  for (int k = 0; k < N; ++k) lam[k] = lam[k] > 0.0 ? lam[k] : 0.0;
+#pragma unroll
   for (int i = 0; i < N; ++i)
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
+    for (int j = i; j < N; ++j) {
       double acc = 0;
 #pragma unroll
-      for (int k = 0; k < N; ++k) acc += lam[k] > 0 ? V[i][k] * lam[k] * V[j][k] : 0.0;
+      for (int k = 0; k < N; ++k) acc += (V[i][k] * lam[k]) * V[j][k];
       S[i][j] = acc;
+      S[j][i] = acc;
     }
   return true;
 }
