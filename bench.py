@@ -15,7 +15,8 @@ C ABI with host buffers (e2e: pinned host state -> device, step, device -> host 
 frame), then one profiled pass (up to 5 frames) for the per-kernel roofline. The CPU
 baseline times the oracle on the first Newton iterations of the first timed frame. N > 1 runs N independent
 replicas (one per GPU; the pile does not shard): value = total frames/s of all ranks
-over the max-over-ranks time.
+over the max-over-ranks time. The line also carries the pile's 200-frame run from rest
+(pile_200), the 200-link chain, the batched and the differentiable-rollout workloads.
 reference arm: the CPU restatement of the reference (oracle/, OpenMP on all host
 cores) on the same checkpoint, each step one frame, bounded by a time budget.
 """
@@ -346,6 +347,33 @@ def chain_line(frames=300, fp64_peak=None):
                                  ", ".join("%.2f" % x for x in secs))}}
 
 
+def pile_run_line(frames=200):
+    """The pile's own 200-frame run: the seeded 1024-icosphere pile from rest (bodies
+    falling, first contacts, compression), frames 1-`frames`, each frame timed with CUDA
+    events on the engine's stream with the state resident. Frames whose lagged friction
+    makes the Newton iteration cycle stop at the workload's per-frame cap and are listed."""
+    from adb_gb300 import scene as S
+    from adb_gb300.abd import ABD
+    sc, cfg = S.sphere_pile(seed=0), S.workload_config("pile")
+    sim = ABD(sc, cfg)
+    dev_ms, newton, trials, capped, mpt, mee = 0.0, 0, 0, [], 0, 0
+    t0 = time.perf_counter()
+    for f in range(frames):
+        st = sim.step(1)
+        if cfg.max_iter_frame and st.newton_iters >= cfg.max_iter_frame:
+            capped.append(f + 1)
+        dev_ms += st.device_ms
+        newton += st.newton_iters
+        trials += st.ls_trials
+        mpt, mee = max(mpt, st.n_pt), max(mee, st.n_ee)
+    wall = time.perf_counter() - t0
+    sim.close()
+    return {"workload": "pile-1024 icosphere-s3, frames 1-%d from rest" % frames, "value": frames / (dev_ms / 1000.0),
+            "unit": "frames/s", "steps": frames, "ms_per_step": dev_ms / frames, "wall_s": wall,
+            "frame_stats": {"newton_iters": newton, "ls_trials": trials, "max_pt": mpt, "max_ee": mee,
+                            "frames_at_newton_cap": capped, "newton_cap_per_frame": cfg.max_iter_frame}}
+
+
 def cpu_baseline_sample(sc, cfg, q0, qd, newton_per_frame, ls_per_frame, sample_iters=6):
     """The CPU restatement on all host cores, timed on a bounded sample of one frame.
 
@@ -497,6 +525,7 @@ def run_gb300(args):
             "autotune": sim.autotune_info(),
         }
         if not args.no_batched:
+            line["pile_200"] = pile_run_line()
             line["chain"] = chain_line(fp64_peak=fp64_peak)
             line["batched"] = batched
             try:
