@@ -31,7 +31,7 @@ class AbdConfig(C.Structure):
                                                                  ("damp_alpha", C.c_double), ("damp_beta", C.c_double),
                                                                  ("pcg_refine", C.c_int), ("pcg_refine_tol", C.c_double),
                                                                  ("solver", C.c_int), ("max_iter_frame", C.c_int),
-                                                                 ("autotune", C.c_int)]
+                                                                 ("autotune", C.c_int), ("tri_direct", C.c_int)]
 
 
 class AbdSceneDesc(C.Structure):

@@ -37,6 +37,7 @@ def make_abd_config(cfg: Config) -> L.AbdConfig:
     c.solver = 1 if cfg.solver == "dense" else 0
     c.max_iter_frame = int(cfg.max_iter_frame)
     c.autotune = int(cfg.autotune)
+    c.tri_direct = int(cfg.tri_direct)
     return c
 
 

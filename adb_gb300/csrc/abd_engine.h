@@ -254,6 +254,10 @@ struct NewtonBufs {
   DBuf<int> grp_body, grp_n, grp_scene, sc_gbeg, sc_gend;  // PCG body groups (pcg_groups)
   std::vector<int> h_sc_beg, h_sc_end;  // body range of each scene (host)
   DBuf<double> dense_A, dense_y;         // dense solve: one scene's matrix and right-hand side
+  // block-tridiagonal direct solve: per-scene flags and counts, per-body link to the next
+  // body, the factor's inverse diagonal blocks, coupling blocks and forward solution
+  DBuf<int> tri_bad, tri_on, pcg_on, tri_cnt, tri_link;
+  DBuf<double> tri_Li, tri_W, tri_y;
   // adjoint: friction-frame Jacobians and contributions per pair, the exact system's
   // blocks, GMRES bases
   DBuf<double> fj_pt, fj_ee, fc_pt, fc_ee, D_ex, ovr_ex, adj_V, adj_Z, adj_w, adj_t, adj_x;
@@ -288,10 +292,19 @@ struct SolveOpts {
   int refine = 0;
   double refine_tol = 1e-8;
   int dense = 0;
+  int tri = 0;  // block-tridiagonal scenes by block Cholesky (tri_solve)
 };
 // on (host, ns): the scenes solved (the others get dq = 0); sc_on is its device copy.
 int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& nb, const SolveOpts& o, const int* sc_on,
               const std::vector<char>& on, double* dq, cudaStream_t s, int* status, int* scene_iters);
+// Block-tridiagonal scenes (tri.cu; after the row-block copy of pcg_solve): tri_classify
+// marks the scenes whose blocks only join consecutive bodies (tri_on, when enable) and the
+// others solved (pcg_on), returning both counts; tri_solve factorizes and solves every run
+// of linked bodies of the tri_on scenes (x, dq = -x) and writes x = 0, dq = -0 for the
+// scenes with sc_on == 0.
+void tri_classify(const Geo& g, PairSet& S, NewtonBufs& B, int enable, const int* sc_on, cudaStream_t s,
+                  int* n_pcg, int* n_tri);
+void tri_solve(const Geo& g, PairSet& S, NewtonBufs& B, const int* sc_on, double* dq, cudaStream_t s);
 // Dense Cholesky solve of each scene's system (after the row-block copy of pcg_solve).
 void dense_solve(const Geo& g, PairSet& S, NewtonBufs& B, const std::vector<char>& on, double* dq, cudaStream_t s);
 // Line-search energy of every scene at the trial configuration (X must hold q + alpha dq):

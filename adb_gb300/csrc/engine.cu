@@ -363,6 +363,7 @@ struct Engine {
     o.refine = cfg.pcg_refine;
     o.refine_tol = cfg.pcg_refine_tol;
     o.dense = cfg.solver == 1;
+    o.tri = cfg.tri_direct;
     return o;
   }
 

@@ -247,6 +247,7 @@ extern "C" int abd_create_from_files(const char* config_json, const char* scene_
   c.max_iter = (int)cfgj.num("max_iter", 1000);
   c.max_iter_frame = (int)cfgj.num("max_iter_frame", 0);
   c.autotune = cfgj.flag("autotune", true);
+  c.tri_direct = cfgj.flag("tri_direct", true);
   c.ground = cfgj.flag("ground", true);
   c.pt = cfgj.flag("pt", true);
   c.ee = cfgj.flag("ee", true);

@@ -2022,6 +2022,14 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, const SolveOpts& o, const
     prof_work(K_BLOCK_INVERSE, 1, 2 * 1152.0 * B.h_int[2]);
     return 0;
   }
+  // block-tridiagonal scenes are solved directly (tri.cu); the CG takes the others
+  int n_pcg = 1, n_tri = 0;
+  const int* pcg_mask = sc_on;
+  if (o.tri) {
+    tri_classify(g, S, B, 1, sc_on, s, &n_pcg, &n_tri);
+    if (n_tri > 0) pcg_mask = B.pcg_on.p;
+  }
+  const bool run_pcg = n_tri == 0 || n_pcg > 0;
   static int max_blocks = 0, max_blocks1 = 0;
   if (!max_blocks) {
     int dev, sms, per, per1;
@@ -2051,7 +2059,7 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, const SolveOpts& o, const
   a.grp_scene = B.grp_scene.p;
   a.sc_gbeg = B.sc_gbeg.p;
   a.sc_gend = B.sc_gend.p;
-  a.sc_on = sc_on;
+  a.sc_on = pcg_mask;
   a.x = B.x.p;
   a.r = B.r.p;
   a.z = B.z.p;
@@ -2070,9 +2078,9 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, const SolveOpts& o, const
   a.out = B.status.p;
   void* args[] = {&a};
   const void* kern = one ? (void*)k_pcg1 : (void*)k_pcg;
-  KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(PCG_NT), args, 0, s)));
+  if (run_pcg) KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(PCG_NT), args, 0, s)));
   const int nrows = 12 * nb;
-  if (refine > 0) {
+  if (run_pcg && refine > 0) {
     // Iterative refinement: the PCG's recurrence residual drifts from b - H x as the
     // iterates converge, so the solution is corrected with the true residual computed
     // from the same row-block matrix, each correction solved by the same PCG to
@@ -2093,23 +2101,30 @@ int pcg_solve(const Geo& g, PairSet& S, NewtonBufs& B, const SolveOpts& o, const
     void* cargs[] = {&c};
     for (int k = 0; k < refine; ++k) {
       KLAUNCH(K_PCG, s, k_true_residual<<<nblk(nrows, 256), 256, 0, s>>>(nb, S.row_ptr.p, B.rcol.p, B.rn.p,
-                                                                         B.Hrow.p, g.bscene, sc_on, B.grad.p,
+                                                                         B.Hrow.p, g.bscene, pcg_mask, B.grad.p,
                                                                          B.xr.p, B.rt.p));
       KLAUNCH(K_PCG, s, CK(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(PCG_NT), cargs, 0, s)));
       KLAUNCH(K_VEC, s, k_refine_add<<<nblk(nrows, 256), 256, 0, s>>>(nrows, B.xr.p, B.x.p, dq));
       KLAUNCH(K_VEC, s, k_iter_add<<<1, 32, 0, s>>>(ns, B.status.p + 1, B.sc_iters.p, B.it_ref.p));
     }
     CK(cudaMemcpyAsync(B.x.p, B.xr.p, nrows * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  }
+  if (n_tri > 0) tri_solve(g, S, B, sc_on, dq, s);
+  CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (run_pcg && refine > 0) {
     CK(cudaMemcpyAsync(B.h_ref.data(), B.it_ref.p, (2 + (size_t)ns) * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     B.h_int[1] = B.h_ref[0];
     if (scene_iters)
       for (int k = 0; k < ns; ++k) scene_iters[k] = B.h_ref[2 + k];
-  } else {
-    CK(cudaMemcpyAsync(B.h_int, B.status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  } else if (run_pcg) {
     if (scene_iters) CK(cudaMemcpyAsync(scene_iters, B.sc_iters.p, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+  } else {
+    CK(cudaStreamSynchronize(s));
+    B.h_int[1] = 0;
+    if (scene_iters)
+      for (int k = 0; k < ns; ++k) scene_iters[k] = 0;
   }
   *status = B.h_int[0];
   // per iteration: the kept blocks once (1152 B each) and ~6 vector streams

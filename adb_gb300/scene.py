@@ -49,6 +49,7 @@ class Config:
     max_iter: int = 1000
     max_iter_frame: int = 0        # Newton iterations per frame at most (0: unbounded, as the reference)
     autotune: bool = True          # narrow-phase launch variants chosen by timing (results unchanged)
+    tri_direct: bool = True        # block-tridiagonal scenes solved by block Cholesky (solver "sparse")
     ground: bool = True
     pt: bool = True
     ee: bool = True
@@ -137,6 +138,7 @@ def load_config(path: str) -> Config:
     c.pcg_refine = int(d.get("pcg_refine", c.pcg_refine))
     c.max_iter_frame = int(d.get("max_iter_frame", c.max_iter_frame))
     c.autotune = bool(d.get("autotune", c.autotune))
+    c.tri_direct = bool(d.get("tri_direct", c.tri_direct))
     c.pcg_refine_tol = float(d.get("pcg_refine_tol", c.pcg_refine_tol))
     return c
 
@@ -159,6 +161,7 @@ def config_to_json(c: Config) -> dict:
         "dhat": c.dhat, "ortho_kappa": c.ortho_kappa, "ground_y": -c.ground_offset,
         "pcg_rel_tol": c.pcg_rel_tol, "pcg_max_iter": c.pcg_max_iter,
         "pcg_refine": c.pcg_refine, "pcg_refine_tol": c.pcg_refine_tol, "max_iter_frame": c.max_iter_frame, "autotune": c.autotune,
+        "tri_direct": c.tri_direct,
     }
 
 

@@ -89,6 +89,12 @@ typedef struct {
    * variants on the same input and keeps the fastest for the handle (results do not
    * depend on the variant); 0: the default variants. No reference counterpart. */
   int autotune;
+  /* 1: with solver 0, a scene whose Newton matrix is block-tridiagonal in body order
+   * (contacts only between consecutive bodies: chains, stacks) is solved directly by a
+   * block Cholesky of each run of linked bodies, as the reference's sparse direct solver
+   * (Pardiso LLT, abd.cpp:233-264) would; other scenes take the PCG. 0: every scene takes
+   * the PCG. No reference counterpart. */
+  int tri_direct;
 } abd_config;
 
 /* Scene: bodies with their rest meshes (local vertex ids per body). */

@@ -58,6 +58,7 @@ def test_pcg_iteration_cap_reports_and_continues(gpu_lib):
     from adb_gb300.abd import ABD
     cfg = S.workload_config("cubes")
     cfg.pcg_max_iter = 1
+    cfg.tri_direct = False   # a stack is block-tridiagonal: keep it on the CG
     sim = ABD(S.cube_stack(4, gap=0.01, seed=2), cfg)
     st = sim.step(3, raise_on_error=False)
     assert st.frames == 3
