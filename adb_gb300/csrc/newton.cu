@@ -399,12 +399,19 @@ __constant__ Sym12Table c_sym12 = Sym12Table();
 // S is symmetric, so for r < s one 3x3 slice M = S[3a+r][3b+s] gives the (r, s) and
 // (s, r) entries of all three blocks (d_A, d_B mirrored; off via M^T), and for r = s
 // only k <= l is formed for d_A and d_B.
-__global__ void __launch_bounds__(128) k_pair_chain(Geo g, int kind, int n, const int* tup, const int* pov,
+// Q's column 1 vanishes on vertices 0 and 1 and its column 0 on vertices 2 and 3, so
+// Y_A's column 1 is zero for both kinds (body A holds vertex 0, and 1 for edge-edge) and
+// Y_B's column 0 is zero for edge-edge pairs: those terms are left out (KIND 0:
+// point-triangle, 1: edge-edge).
+template <int KIND>
+__global__ void __launch_bounds__(128) k_pair_chain(Geo g, int n, const int* tup, const int* pov,
                                                     const int* ovI, const double* R, double* C) {
+  constexpr int kind = KIND;
+  constexpr int na = KIND ? 2 : 1;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  int vid[4], na, A, B;
-  pair_vertices(g, kind, tup, p, vid, na, A, B);
+  int vid[4], na_, A, B;
+  pair_vertices(g, kind, tup, p, vid, na_, A, B);
   if (!scene_on(g, A)) return;
   const size_t N = n;
   const int I = ovI[pov[p]];
@@ -439,6 +446,9 @@ __global__ void __launch_bounds__(128) k_pair_chain(Geo g, int kind, int n, cons
     xt[i][2] = g.rest[3 * vid[i] + 1];
     xt[i][3] = g.rest[3 * vid[i] + 2];
   }
+  // nonzero columns of Y_A and Y_B
+  auto a_nz = [](int c) { return c != 1; };
+  auto b_nz = [](int c) { return KIND == 0 || c != 0; };
   // Y matrices of the chain rule
   double YA[4][3], YB[4][3];
 #pragma unroll
@@ -448,6 +458,7 @@ __global__ void __launch_bounds__(128) k_pair_chain(Geo g, int kind, int n, cons
       double sa = 0, sb = 0;
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
+        if (Qe(i, aa) == 0.0) continue;  // a compile-time zero of Q
         double v = xt[i][k] * Qe(i, aa);
         if (i < na) sa += v;
         else sb += v;
@@ -480,9 +491,34 @@ __global__ void __launch_bounds__(128) k_pair_chain(Geo g, int kind, int n, cons
       for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int bb = 0; bb < 3; ++bb) {
-          TA[k][bb] = YA[k][0] * M[0][bb] + YA[k][1] * M[1][bb] + YA[k][2] * M[2][bb];
-          TB[k][bb] = YB[k][0] * M[0][bb] + YB[k][1] * M[1][bb] + YB[k][2] * M[2][bb];
+          double ta = 0.0, tb = 0.0;
+          bool fa = true, fb = true;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            if (a_nz(c)) {
+              ta = fa ? YA[k][c] * M[c][bb] : ta + YA[k][c] * M[c][bb];
+              fa = false;
+            }
+            if (b_nz(c)) {
+              tb = fb ? YB[k][c] * M[c][bb] : tb + YB[k][c] * M[c][bb];
+              fb = false;
+            }
+          }
+          TA[k][bb] = ta;
+          TB[k][bb] = tb;
         }
+      // u . v over the columns where Y (of `side`: 0 A, 1 B) is nonzero
+      auto dotY = [&](const double (&u)[3], const double (&v)[3], int side) {
+        double acc = 0.0;
+        bool first = true;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          if (side == 0 ? !a_nz(c) : !b_nz(c)) continue;
+          acc = first ? u[c] * v[c] : acc + u[c] * v[c];
+          first = false;
+        }
+        return acc;
+      };
 #pragma unroll
       for (int k = 0; k < 4; ++k)
 #pragma unroll
@@ -490,20 +526,20 @@ __global__ void __launch_bounds__(128) k_pair_chain(Geo g, int kind, int n, cons
           const int e = (3 * k + r) * 12 + (3 * l + s);
           const int et = (3 * l + s) * 12 + (3 * k + r);
           if (r < s || k <= l) {
-            double aa_ = TA[k][0] * YA[l][0] + TA[k][1] * YA[l][1] + TA[k][2] * YA[l][2];
-            double bb_ = TB[k][0] * YB[l][0] + TB[k][1] * YB[l][1] + TB[k][2] * YB[l][2];
+            double aa_ = dotY(TA[k], YA[l], 0);
+            double bb_ = dotY(TB[k], YB[l], 1);
             const int ui = c_sym12.v[e];  // the same entry for the whole warp
             dA[ui * N + p] = a_dyn ? aa_ : 0.0;
             dB[ui * N + p] = b_dyn ? bb_ : 0.0;
           }
           // (A row (k, r), B column (l, s)), stored as block (I, J)
-          double ab_ = TA[k][0] * YB[l][0] + TA[k][1] * YB[l][1] + TA[k][2] * YB[l][2];
+          double ab_ = dotY(TA[k], YB[l], 1);
           off[(a_is_I ? e : et) * N + p] = off_on ? ab_ : 0.0;
           if (r < s) {
             // (A row (k, s), B column (l, r)) = Y_A[k] M^T Y_B[l]^T
             const int e2 = (3 * k + s) * 12 + (3 * l + r);
             const int et2 = (3 * l + r) * 12 + (3 * k + s);
-            double ba_ = TB[l][0] * YA[k][0] + TB[l][1] * YA[k][1] + TB[l][2] * YA[k][2];
+            double ba_ = dotY(TB[l], YA[k], 0);
             off[(a_is_I ? e2 : et2) * N + p] = off_on ? ba_ : 0.0;
           }
         }
@@ -1964,9 +2000,12 @@ void assemble(const Geo& g, const Params& P, PairSet& S, NewtonBufs& B, cudaStre
     KLAUNCH(K_PAIR_TERMS, s, k_pair_hess<<<nblk(n, 128), 128, 0, s>>>(g, P, kind, n, tup, ty, B.perm.p, n_moll,
                                                                     B.prec.p, kind ? S.ee_lag.p : S.pt_lag.p));
     if (kind) CK(cudaStreamWaitEvent(s, B.ev_join, 0));
-    KLAUNCH(K_PAIR_TERMS, s, k_pair_chain<<<nblk(n, 128), 128, 0, s>>>(g, kind, n, tup, kind ? S.ee_ov.p : S.pt_ov.p,
-                                                                     S.ovI.p, B.prec.p,
-                                                                     kind ? B.ee_c.p : B.pt_c.p));
+    if (kind)
+      KLAUNCH(K_PAIR_TERMS, s, k_pair_chain<1><<<nblk(n, 128), 128, 0, s>>>(g, n, tup, S.ee_ov.p, S.ovI.p, B.prec.p,
+                                                                            B.ee_c.p));
+    else
+      KLAUNCH(K_PAIR_TERMS, s, k_pair_chain<0><<<nblk(n, 128), 128, 0, s>>>(g, n, tup, S.pt_ov.p, S.ovI.p, B.prec.p,
+                                                                            B.pt_c.p));
   }
   if (nov) {
     KLAUNCH(K_SEG, s, k_seg<<<nblk(nov + 1, 256), 256, 0, s>>>(nov, npt, S.pt_ov.p, B.pt_seg.p));
