@@ -41,6 +41,21 @@ def test_config_parse(tmp_path):
     assert back["uppper_bound"] and back["params_double"]["tol"] == 1e-4
 
 
+def test_config_library_keys_roundtrip(tmp_path):
+    """Keys with no reference counterpart survive the JSON front end both ways."""
+    c = S.workload_config("chain")
+    c.tri_direct, c.autotune, c.solver = False, False, "dense"
+    p = tmp_path / "config.json"
+    p.write_text(json.dumps(S.config_to_json(c)))
+    b = S.load_config(str(p))
+    assert (b.tri_direct, b.autotune, b.solver, b.max_iter_frame) == (False, False, "dense", 100)
+    assert S.load_config(str(p)).pcg_rel_tol == c.pcg_rel_tol
+    d = json.loads(p.read_text())
+    del d["tri_direct"]
+    p.write_text(json.dumps(d))
+    assert S.load_config(str(p)).tri_direct   # default on
+
+
 def test_scene_json_roundtrip(tmp_path):
     S.write_obj(str(tmp_path / "ico.obj"), S.icosphere_mesh(1))
     entries = [
