@@ -293,10 +293,26 @@ __global__ void __launch_bounds__(32 * MOLL_W) k_pair_moll(Geo g, Params P, int 
                   __syncwarp();
                   continue;
                 }
+                // rotation parameters from two reciprocal square roots (g = 1 / r,
+                // c^2 = (|h| + r) / (2 r), t = sgn(h) a g / (2 c^2), s = sgn(h) a g / (2 c)),
+                // as in psd_project_small; by division below the normal range
                 const double h = 0.5 * (aqq - app);
-                const double den = fabs(h) + sqrt(h * h + apq * apq);
-                const double tt = den > 0.0 ? (h >= 0 ? apq : -apq) / den : 0.0;
-                const double c = rsqrt(1.0 + tt * tt), sn = tt * c;
+                const double sa = h >= 0 ? apq : -apq;
+                const double r2 = fma(h, h, apq * apq);
+                double tt, c, sn;
+                if (r2 >= 1e-300) {
+                  const double g = rsqrt(r2);
+                  const double c2 = 0.5 * fma(r2, g, fabs(h)) * g;
+                  const double ic = rsqrt(c2);
+                  sn = 0.5 * sa * g * ic;
+                  c = c2 * ic;
+                  tt = sn * ic;
+                } else {
+                  const double den = fabs(h) + sqrt(r2);
+                  tt = den > 0.0 ? sa / den : 0.0;
+                  c = rsqrt(1.0 + tt * tt);
+                  sn = tt * c;
+                }
                 __syncwarp();
                 if (lane < 9 && lane != pp && lane != qq) {
                   const double akp = A[lane][pp], akq = A[lane][qq];
